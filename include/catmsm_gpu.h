@@ -1,0 +1,130 @@
+/*
+ * catmsm-gb300: BLS12-381 G1 multi-scalar multiplication and G1 group FFT on
+ * one sm_103a GPU, behind the category-blst C ABI.
+ *
+ * Part 1 declares the drop-in entry points.  Each has the exact name,
+ * signature, argument meaning and fail-closed behaviour of the reference
+ * function cited beside it (paths are within the reference project).  All
+ * buffers are caller-owned HOST memory; every call is synchronous; no
+ * exception or abort crosses the boundary.  Device memory, streams and
+ * pinned staging are owned per calling thread inside the library.
+ *
+ * Part 2 declares device-resident and tooling entry points that have no
+ * reference counterpart (resident inputs for serving/benchmarks, seeded
+ * input generation, field self-checks).
+ */
+#ifndef CATMSM_GPU_H
+#define CATMSM_GPU_H
+
+#include <stdbool.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Reference ABI types (bindings/blst_types.h:40-103), byte-identical. */
+typedef uint8_t blst_byte;
+typedef uint64_t blst_limb_t;
+typedef struct { blst_limb_t l[4]; } blst_fr;             /* Montgomery, R = 2^256 */
+typedef struct { blst_limb_t l[6]; } blst_fp;             /* Montgomery, R = 2^384 */
+typedef struct { blst_fp x, y, z; } blst_p1;              /* Jacobian; z == 0 is infinity */
+typedef struct { blst_fp x, y; } blst_p1_affine;          /* all-zero is infinity */
+
+/* ------------------------------------------------------------------ Part 1 */
+
+/* Replaces blst_p1s_mult_pippenger_scratch_sizeof
+ * (bindings/blst_scalar.h:535, blst/c_api.cpp:1371).  Returns the reference's
+ * value, 192 * 2^(c(n)-1) bytes (0 for n = 0), so callers size scratch as
+ * before; the GPU path itself does not touch the scratch. */
+size_t blst_p1s_mult_pippenger_scratch_sizeof(size_t npoints);
+
+/* Replaces blst_p1s_mult_pippenger_window_scratch_sizeof
+ * (bindings/blst_scalar.h:537, blst/c_api.cpp:1376): 0 for window outside [1, 24]. */
+size_t blst_p1s_mult_pippenger_window_scratch_sizeof(size_t window);
+
+/* Replaces blst_p1s_mult_pippenger (bindings/blst_scalar.h:539,
+ * blst/c_api.cpp:1382-1418).  ret = sum_i k_i * P_i, k_i the low nbits bits
+ * of scalars[i] (ceil(nbits/8) little-endian bytes).  Descriptor arrays:
+ * a later NULL entry means contiguous continuation from the previous entry
+ * (blst/scalar/curve/multi_scalar.cpp:838-841); exact n-entry arrays are read
+ * without a sentinel.  npoints == 0 or nbits == 0 -> infinity; nbits > 256 or
+ * a NULL head pointer -> infinity; npoints > 1 with scratch == NULL ->
+ * infinity; a device failure also writes infinity.  The result is written
+ * normalised (z = Montgomery one, or all-zero for infinity). */
+void blst_p1s_mult_pippenger(blst_p1 *ret, const blst_p1_affine *const points[], size_t npoints,
+                             const blst_byte *const scalars[], size_t nbits, blst_limb_t *scratch);
+
+/* Replaces blst_p1s_mult_pippenger_window (bindings/blst_scalar.h:603,
+ * blst/c_api.cpp:1546-1583): as above; window outside [1, 24] -> infinity.
+ * The window is accepted for validation only: the GPU picks its own width,
+ * which leaves the result (a group element) unchanged. */
+void blst_p1s_mult_pippenger_window(blst_p1 *ret, const blst_p1_affine *const points[], size_t npoints,
+                                    const blst_byte *const scalars[], size_t nbits, blst_limb_t *scratch,
+                                    size_t window);
+
+/* Replaces blst_fr_fft_domain_len (bindings/blst_fft.h:52, blst/fft_c_api.cpp:128):
+ * n + 2 for n a power of two in [1, 2^30], else 0. */
+size_t blst_fr_fft_domain_len(size_t n);
+
+/* Replaces blst_fr_fft_domain_init (bindings/blst_fft.h:65, blst/fft_c_api.cpp:133-146):
+ * domain = [w^0 .. w^(n-1), 1/n, n] in Montgomery form, w the reference's
+ * primitive n-th root.  false (contents unspecified) on a bad length/size. */
+bool blst_fr_fft_domain_init(blst_fr *domain, size_t domain_len, size_t n);
+
+/* Replaces blst_p1_fft (bindings/blst_fft.h:109, blst/fft_c_api.cpp:184 -> :51-66):
+ * in-place natural-order G1 DFT with powers of the primitive n-th root
+ * (inverse: of its reciprocal, then scaled by 1/n).  false before writing on
+ * NULL values or invalid n; false with values untouched on a device failure. */
+bool blst_p1_fft(blst_p1 *values, size_t n, bool inverse);
+
+/* Replaces blst_p1_fft_with_domain (bindings/blst_fft.h:111, blst/fft_c_api.cpp:194 ->
+ * :68-103): domain_len must be n + 2 and domain[n+1] the Montgomery tag n, else
+ * false before writing; inverse reads forward roots at n - idx and scales by
+ * domain[n]. */
+bool blst_p1_fft_with_domain(blst_p1 *values, size_t n, const blst_fr *domain, size_t domain_len,
+                             bool inverse);
+
+/* Replaces blst_p1_ifft_unscaled_with_domain (bindings/blst_fft.h:131,
+ * blst/fft_c_api.cpp:208): the inverse transform without the 1/n scale. */
+bool blst_p1_ifft_unscaled_with_domain(blst_p1 *values, size_t n, const blst_fr *domain, size_t domain_len);
+
+/* ------------------------------------------------------------------ Part 2 */
+
+/* MSM over DEVICE-resident inputs (no reference counterpart): d_points is n
+ * contiguous affine points, d_scalars n scalars of `stride` bytes (nbits used),
+ * all in device memory of the current device; window 0 = library default.
+ * Runs on the calling thread's library stream; the result lands in host *ret.
+ * Returns 0 on success, else a cudaError_t value (ret set to infinity). */
+int catmsm_p1s_mult_pippenger_device(blst_p1 *ret, const void *d_points, const void *d_scalars,
+                                     size_t stride, size_t npoints, size_t nbits, size_t window);
+
+/* G1 FFT over DEVICE-resident Jacobian values with a DEVICE-resident domain
+ * (n + 2 Montgomery Fr, as built by blst_fr_fft_domain_init).  mode 0:
+ * forward, 1: inverse (scaled), 2: inverse unscaled.  Returns 0 on success. */
+int catmsm_p1_fft_device(void *d_values, size_t n, const void *d_domain, int mode);
+
+/* The calling thread's library CUDA stream (cudaStream_t), for event timing. */
+void *catmsm_stream(void);
+
+/* Number of kernels this thread launched through the library so far. */
+long catmsm_launch_count(void);
+
+/* The window width the GPU MSM uses for n points. */
+size_t catmsm_msm_window(size_t npoints);
+
+/* Seeded-input support: out[i] = k_i * G (affine, canonical) for n 32-byte
+ * little-endian scalars.  Host buffers; returns 0 on success. */
+int catmsm_p1_affines_from_scalars(blst_p1_affine *out, const blst_byte *k32, size_t n);
+/* Same with device buffers on the library stream. */
+int catmsm_p1_affines_from_scalars_device(void *d_out, const void *d_k32, size_t n);
+
+/* Field self-check: out[i] = a[i] * b[i] * R^-1 mod p (canonical), host
+ * buffers of n blst_fp.  Returns 0 on success. */
+int catmsm_fp_mul(blst_fp *out, const blst_fp *a, const blst_fp *b, size_t n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

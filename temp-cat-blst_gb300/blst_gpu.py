@@ -1,0 +1,198 @@
+"""Python mirror of the library's C ABI (ctypes over libcatmsm_gpu.so).
+
+Function names, argument meaning and failure behaviour follow the reference's
+C entry points (bindings/blst_scalar.h:535-539, :603; bindings/blst_fft.h:52-131):
+the MSM returns the point at infinity on invalid input, the FFT calls return
+False and leave the values unchanged.  Buffers are ``bytes``/``bytearray`` in
+the reference ABI layouts (96-byte affine points, 144-byte Jacobian points,
+32-byte scalars, 32-byte Montgomery Fr).
+
+Loading fails loudly when the shared library is missing or cannot be built:
+there is no CPU fallback.
+"""
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libcatmsm_gpu.so")
+
+P1 = 144
+P1A = 96
+FR = 32
+
+_vp = C.c_void_p
+_sz = C.c_size_t
+
+_lib = None
+
+
+def load(build_if_missing=True):
+    """Load (building first if needed) the CUDA library; raises on failure."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if build_if_missing:
+        import importlib.util
+        spec = importlib.util.spec_from_file_location("catmsm_build", os.path.join(HERE, "build.py"))
+        mod = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mod)
+        mod.build()
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError("libcatmsm_gpu.so is missing; run build.py")
+    L = C.CDLL(LIB_PATH)
+    L.blst_p1s_mult_pippenger_scratch_sizeof.restype = _sz
+    L.blst_p1s_mult_pippenger_scratch_sizeof.argtypes = [_sz]
+    L.blst_p1s_mult_pippenger_window_scratch_sizeof.restype = _sz
+    L.blst_p1s_mult_pippenger_window_scratch_sizeof.argtypes = [_sz]
+    L.blst_p1s_mult_pippenger.restype = None
+    L.blst_p1s_mult_pippenger.argtypes = [_vp, _vp, _sz, _vp, _sz, _vp]
+    L.blst_p1s_mult_pippenger_window.restype = None
+    L.blst_p1s_mult_pippenger_window.argtypes = [_vp, _vp, _sz, _vp, _sz, _vp, _sz]
+    L.blst_fr_fft_domain_len.restype = _sz
+    L.blst_fr_fft_domain_len.argtypes = [_sz]
+    L.blst_fr_fft_domain_init.restype = C.c_bool
+    L.blst_fr_fft_domain_init.argtypes = [_vp, _sz, _sz]
+    L.blst_p1_fft.restype = C.c_bool
+    L.blst_p1_fft.argtypes = [_vp, _sz, C.c_bool]
+    L.blst_p1_fft_with_domain.restype = C.c_bool
+    L.blst_p1_fft_with_domain.argtypes = [_vp, _sz, _vp, _sz, C.c_bool]
+    L.blst_p1_ifft_unscaled_with_domain.restype = C.c_bool
+    L.blst_p1_ifft_unscaled_with_domain.argtypes = [_vp, _sz, _vp, _sz]
+    L.catmsm_p1s_mult_pippenger_device.restype = C.c_int
+    L.catmsm_p1s_mult_pippenger_device.argtypes = [_vp, _vp, _vp, _sz, _sz, _sz, _sz]
+    L.catmsm_p1_fft_device.restype = C.c_int
+    L.catmsm_p1_fft_device.argtypes = [_vp, _sz, _vp, C.c_int]
+    L.catmsm_stream.restype = _vp
+    L.catmsm_stream.argtypes = []
+    L.catmsm_launch_count.restype = C.c_long
+    L.catmsm_launch_count.argtypes = []
+    L.catmsm_msm_window.restype = _sz
+    L.catmsm_msm_window.argtypes = [_sz]
+    L.catmsm_p1_affines_from_scalars.restype = C.c_int
+    L.catmsm_p1_affines_from_scalars.argtypes = [_vp, _vp, _sz]
+    L.catmsm_p1_affines_from_scalars_device.restype = C.c_int
+    L.catmsm_p1_affines_from_scalars_device.argtypes = [_vp, _vp, _sz]
+    L.catmsm_fp_mul.restype = C.c_int
+    L.catmsm_fp_mul.argtypes = [_vp, _vp, _vp, _sz]
+    _lib = L
+    return L
+
+
+def _buf(data):
+    if isinstance(data, bytearray):
+        return (C.c_char * len(data)).from_buffer(data)
+    return C.c_char_p(bytes(data))
+
+
+def _addr(b):
+    return C.cast(b, C.c_void_p)
+
+
+def p1s_mult_pippenger(points: bytes, scalars: bytes, npoints: int, nbits: int = 255,
+                       scratch: bool = True) -> bytes:
+    """Contiguous-descriptor MSM through the C ABI; returns the 144-byte blst_p1."""
+    L = load()
+    pb = _buf(bytearray(points) if points else bytearray(96))
+    sb = _buf(bytearray(scalars) if scalars else bytearray(32))
+    parr = (C.c_void_p * 2)(_addr(pb), None)
+    sarr = (C.c_void_p * 2)(_addr(sb), None)
+    scr = (C.c_uint64 * 4)() if scratch else None
+    ret = bytearray(P1)
+    L.blst_p1s_mult_pippenger(_buf(ret), parr, npoints, sarr, nbits, scr)
+    return bytes(ret)
+
+
+def p1s_mult_pippenger_descriptors(point_ptrs, scalar_ptrs, npoints, nbits, scratch=True, window=None) -> bytes:
+    """MSM with caller-built descriptor arrays (lists of addresses or None)."""
+    L = load()
+    parr = (C.c_void_p * len(point_ptrs))(*point_ptrs)
+    sarr = (C.c_void_p * len(scalar_ptrs))(*scalar_ptrs)
+    scr = (C.c_uint64 * 4)() if scratch else None
+    ret = bytearray(P1)
+    if window is None:
+        L.blst_p1s_mult_pippenger(_buf(ret), parr, npoints, sarr, nbits, scr)
+    else:
+        L.blst_p1s_mult_pippenger_window(_buf(ret), parr, npoints, sarr, nbits, scr, window)
+    return bytes(ret)
+
+
+def scratch_sizeof(n: int) -> int:
+    return load().blst_p1s_mult_pippenger_scratch_sizeof(n)
+
+
+def window_scratch_sizeof(w: int) -> int:
+    return load().blst_p1s_mult_pippenger_window_scratch_sizeof(w)
+
+
+def fr_fft_domain_len(n: int) -> int:
+    return load().blst_fr_fft_domain_len(n)
+
+
+def fr_fft_domain_init(n: int, domain_len: int = None):
+    L = load()
+    dl = L.blst_fr_fft_domain_len(n) if domain_len is None else domain_len
+    out = bytearray(FR * max(dl, 1))
+    ok = L.blst_fr_fft_domain_init(_buf(out), dl, n)
+    return ok, bytes(out)
+
+
+def p1_fft(values: bytes, n: int, inverse: bool):
+    b = bytearray(values)
+    ok = load().blst_p1_fft(_buf(b) if b else None, n, inverse)
+    return ok, bytes(b)
+
+
+def p1_fft_with_domain(values: bytes, n: int, domain: bytes, domain_len: int, inverse: bool):
+    b = bytearray(values)
+    ok = load().blst_p1_fft_with_domain(_buf(b) if b else None, n, _buf(domain) if domain else None,
+                                        domain_len, inverse)
+    return ok, bytes(b)
+
+
+def p1_ifft_unscaled_with_domain(values: bytes, n: int, domain: bytes, domain_len: int):
+    b = bytearray(values)
+    ok = load().blst_p1_ifft_unscaled_with_domain(_buf(b) if b else None, n, _buf(domain) if domain else None,
+                                                  domain_len)
+    return ok, bytes(b)
+
+
+def points_from_scalars(k32: bytes, n: int) -> bytes:
+    out = bytearray(P1A * n)
+    rc = load().catmsm_p1_affines_from_scalars(_buf(out), _buf(k32), n)
+    if rc != 0:
+        raise RuntimeError("catmsm_p1_affines_from_scalars failed: %d" % rc)
+    return bytes(out)
+
+
+def fp_mul(a: bytes, b: bytes, n: int) -> bytes:
+    out = bytearray(48 * n)
+    rc = load().catmsm_fp_mul(_buf(out), _buf(a), _buf(b), n)
+    if rc != 0:
+        raise RuntimeError("catmsm_fp_mul failed: %d" % rc)
+    return bytes(out)
+
+
+def msm_device(d_points: int, d_scalars: int, stride: int, n: int, nbits: int, window: int = 0) -> bytes:
+    ret = bytearray(P1)
+    rc = load().catmsm_p1s_mult_pippenger_device(_buf(ret), d_points, d_scalars, stride, n, nbits, window)
+    if rc != 0:
+        raise RuntimeError("catmsm_p1s_mult_pippenger_device failed: %d" % rc)
+    return bytes(ret)
+
+
+def fft_device(d_values: int, n: int, d_domain: int, mode: int) -> None:
+    rc = load().catmsm_p1_fft_device(d_values, n, d_domain, mode)
+    if rc != 0:
+        raise RuntimeError("catmsm_p1_fft_device failed: %d" % rc)
+
+
+def stream_handle() -> int:
+    return load().catmsm_stream()
+
+
+def launch_count() -> int:
+    return load().catmsm_launch_count()
+
+
+def msm_window(n: int) -> int:
+    return load().catmsm_msm_window(n)

@@ -1,0 +1,347 @@
+// C-ABI boundary: the category-blst entry points for the G1 MSM and the G1
+// FFT (declared in include/catmsm_gpu.h with the reference file:line each one
+// replaces), plus the device-resident extensions.  Every entry point runs on
+// the calling thread's own stream and workspaces, is synchronous, and fails
+// closed exactly like the reference: the MSM writes infinity, the FFT returns
+// false with the caller's values untouched.
+#include "common.cuh"
+#include "catmsm_internal.h"
+#include "host_curve.hpp"
+#include "host_fr.hpp"
+#include "../../include/catmsm_gpu.h"
+
+#include <climits>
+#include <cstring>
+#include <new>
+
+namespace catmsm {
+
+Ctx* get_ctx()
+{
+    static thread_local Ctx* per_dev[64] = {nullptr};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+    if (!per_dev[dev]) {
+        Ctx* c = new (std::nothrow) Ctx();
+        if (!c) return nullptr;
+        c->device = dev;
+        if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+            delete c;
+            return nullptr;
+        }
+        per_dev[dev] = c;
+    }
+    return per_dev[dev];
+}
+
+// Reference window heuristic (multi_scalar.h:329-348), used only for the
+// scratch-size contract.
+static size_t ref_window(size_t n)
+{
+    size_t w;
+    for (w = 0; n >>= 1; w++) {}
+    if (w > 12) w -= 3;
+    else if (w > 8) w -= 2;
+    else if (w > 4) w -= 1;
+    else return w ? 2 : 1;
+    return w < 24 ? w : 24;
+}
+
+static bool valid_fft_size(size_t n) { return n != 0 && (n & (n - 1)) == 0 && n <= (size_t)INT_MAX; }
+
+static unsigned log2_exact(size_t n)
+{
+    unsigned k = 0;
+    while (((size_t)1 << k) < n) k++;
+    return k;
+}
+
+// Gather the descriptor walk of multi_scalar.cpp:830-841 into contiguous
+// host staging; returns the contiguous base directly when possible.
+template <typename T>
+static const uint8_t* gather(const T* const arr[], size_t n, size_t elem, PinnedBuf& stage, bool& err)
+{
+    err = false;
+    if (n == 1 || arr[1] == nullptr) return reinterpret_cast<const uint8_t*>(arr[0]);
+    uint8_t* dst = (uint8_t*)stage.get(n * elem);
+    if (!dst) { err = true; return nullptr; }
+    const uint8_t* cur = reinterpret_cast<const uint8_t*>(arr[0]);
+    const T* const* next = arr + 1;
+    std::memcpy(dst, cur, elem);
+    for (size_t i = 1; i < n; i++) {
+        if (*next) cur = reinterpret_cast<const uint8_t*>(*next++);
+        else cur += elem;
+        std::memcpy(dst + i * elem, cur, elem);
+    }
+    return dst;
+}
+
+static void write_inf(blst_p1* ret) { std::memset(ret, 0, sizeof(*ret)); }
+
+static void msm_entry(blst_p1* ret, const blst_p1_affine* const points[], size_t npoints,
+                      const blst_byte* const scalars[], size_t nbits, blst_limb_t* scratch, bool explicit_window,
+                      size_t window)
+{
+    if (!ret) return;
+    if (npoints == 0 || nbits == 0) { write_inf(ret); return; }
+    if (nbits > 256 || (explicit_window && (window < 1 || window > 24)) || !points || !scalars ||
+        !points[0] || !scalars[0]) {
+        write_inf(ret);
+        return;
+    }
+    if (npoints > 1 && scratch == nullptr) { write_inf(ret); return; }
+    if (npoints > 0x7fffffffu) { write_inf(ret); return; }
+    Ctx* ctx = get_ctx();
+    if (!ctx) { write_inf(ret); return; }
+    const size_t nbytes = (nbits + 7) / 8;
+    bool e1, e2;
+    const uint8_t* hp = gather(points, npoints, sizeof(blst_p1_affine), ctx->h_points, e1);
+    const uint8_t* hs = gather(scalars, npoints, nbytes, ctx->h_scalars, e2);
+    if (e1 || e2) { write_inf(ret); return; }
+    void* dp = ctx->msm.points.get(npoints * sizeof(blst_p1_affine));
+    void* ds = ctx->msm.scalars.get(npoints * nbytes + 16);
+    if (!dp || !ds) { write_inf(ret); return; }
+    uint64_t out[18];
+    cudaError_t err = cudaMemcpyAsync(dp, hp, npoints * sizeof(blst_p1_affine), cudaMemcpyHostToDevice, ctx->stream);
+    if (err == cudaSuccess)
+        err = cudaMemcpyAsync(ds, hs, npoints * nbytes, cudaMemcpyHostToDevice, ctx->stream);
+    if (err == cudaSuccess)
+        err = msm_device(ctx, dp, (const uint8_t*)ds, (uint32_t)nbytes, npoints, (uint32_t)nbits, 0, out);
+    if (err != cudaSuccess) { write_inf(ret); return; }
+    std::memcpy(ret, out, sizeof(*ret));
+}
+
+// Common FFT driver.  domain == nullptr: one-shot (roots built from the
+// primitive root, or its inverse); else the caller's prepared domain.
+static bool fft_entry(blst_p1* values, size_t n, const blst_fr* domain, bool inverse, bool scaled)
+{
+    using namespace catmsm_host;
+    Ctx* ctx = get_ctx();
+    if (!ctx) return false;
+    cudaStream_t st = ctx->stream;
+    FftWork& W = ctx->fft;
+    void* dv = W.values.get(n * sizeof(blst_p1));
+    uint32_t* dr = (uint32_t*)W.roots.get((n + 2) * sizeof(blst_fr));
+    if (!dv || !dr) return false;
+    cudaError_t err = cudaSuccess;
+    const uint32_t* scale = nullptr;
+    bool inv_from_fwd = false;
+    if (domain) {
+        err = cudaMemcpyAsync(dr, domain, (n + 1) * sizeof(blst_fr), cudaMemcpyHostToDevice, st);
+        inv_from_fwd = inverse;
+        if (inverse && scaled) scale = dr + 8 * n;
+    } else {
+        hfr w = fr_root_of_unity(log2_exact(n));
+        if (inverse) w = fr_inv(w);
+        hfr* hw = (hfr*)ctx->h_out.get(2 * sizeof(hfr));
+        if (!hw) return false;
+        hw[0] = w;
+        hw[1] = fr_inv(fr_from_u64(n));
+        err = cudaMemcpyAsync(dr + 8 * n, hw, 2 * sizeof(hfr), cudaMemcpyHostToDevice, st);
+        if (err == cudaSuccess) err = fft_root_powers(ctx, dr + 8 * n, n, dr);
+        if (err == cudaSuccess && inverse) {
+            err = cudaMemcpyAsync(dr + 8 * n, dr + 8 * n + 8, sizeof(hfr), cudaMemcpyDeviceToDevice, st);
+            scale = dr + 8 * n;
+        }
+    }
+    if (err == cudaSuccess) err = cudaMemcpyAsync(dv, values, n * sizeof(blst_p1), cudaMemcpyHostToDevice, st);
+    if (err == cudaSuccess) err = fft_run(ctx, dv, n, dr, inv_from_fwd, scale);
+    // Results go to pinned staging first so a late failure leaves values untouched.
+    void* hstage = nullptr;
+    if (err == cudaSuccess) {
+        hstage = ctx->h_values.get(n * sizeof(blst_p1));
+        if (!hstage) err = cudaErrorMemoryAllocation;
+    }
+    if (err == cudaSuccess) err = cudaMemcpyAsync(hstage, dv, n * sizeof(blst_p1), cudaMemcpyDeviceToHost, st);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(st);
+    if (err != cudaSuccess) return false;
+    std::memcpy(values, hstage, n * sizeof(blst_p1));
+    return true;
+}
+
+static bool domain_tag_ok(size_t n, const blst_fr* domain, size_t domain_len)
+{
+    if (!domain || !valid_fft_size(n) || domain_len != n + 2) return false;
+    catmsm_host::hfr tag = catmsm_host::fr_from_u64(n);
+    return std::memcmp(&domain[n + 1], tag.l, 32) == 0;
+}
+
+}  // namespace catmsm
+
+using namespace catmsm;
+
+extern "C" {
+
+size_t blst_p1s_mult_pippenger_scratch_sizeof(size_t npoints)
+{
+    if (npoints == 0) return 0;
+    return (size_t)192 << (ref_window(npoints) - 1);
+}
+
+size_t blst_p1s_mult_pippenger_window_scratch_sizeof(size_t window)
+{
+    if (window < 1 || window > 24) return 0;
+    return (size_t)192 << (window - 1);
+}
+
+void blst_p1s_mult_pippenger(blst_p1* ret, const blst_p1_affine* const points[], size_t npoints,
+                             const blst_byte* const scalars[], size_t nbits, blst_limb_t* scratch)
+{
+    try {
+        msm_entry(ret, points, npoints, scalars, nbits, scratch, false, 0);
+    } catch (...) {
+        if (ret) write_inf(ret);
+    }
+}
+
+void blst_p1s_mult_pippenger_window(blst_p1* ret, const blst_p1_affine* const points[], size_t npoints,
+                                    const blst_byte* const scalars[], size_t nbits, blst_limb_t* scratch,
+                                    size_t window)
+{
+    try {
+        msm_entry(ret, points, npoints, scalars, nbits, scratch, true, window);
+    } catch (...) {
+        if (ret) write_inf(ret);
+    }
+}
+
+size_t blst_fr_fft_domain_len(size_t n) { return valid_fft_size(n) ? n + 2 : 0; }
+
+bool blst_fr_fft_domain_init(blst_fr* domain, size_t domain_len, size_t n)
+{
+    using namespace catmsm_host;
+    try {
+        if (!domain || !valid_fft_size(n) || domain_len != n + 2) return false;
+        Ctx* ctx = get_ctx();
+        if (!ctx) return false;
+        uint32_t* dr = (uint32_t*)ctx->fft.roots.get((n + 1) * sizeof(blst_fr));
+        hfr* hw = (hfr*)ctx->h_out.get(sizeof(hfr));
+        if (!dr || !hw) return false;
+        hw[0] = fr_root_of_unity(log2_exact(n));
+        cudaError_t err = cudaMemcpyAsync(dr + 8 * n, hw, sizeof(hfr), cudaMemcpyHostToDevice, ctx->stream);
+        if (err == cudaSuccess) err = fft_root_powers(ctx, dr + 8 * n, n, dr);
+        if (err == cudaSuccess)
+            err = cudaMemcpyAsync(domain, dr, n * sizeof(blst_fr), cudaMemcpyDeviceToHost, ctx->stream);
+        if (err == cudaSuccess) err = cudaStreamSynchronize(ctx->stream);
+        if (err != cudaSuccess) return false;
+        hfr nn = fr_from_u64(n);
+        hfr inv = fr_inv(nn);
+        std::memcpy(&domain[n], inv.l, 32);
+        std::memcpy(&domain[n + 1], nn.l, 32);
+        return true;
+    } catch (...) {
+        return false;
+    }
+}
+
+bool blst_p1_fft(blst_p1* values, size_t n, bool inverse)
+{
+    try {
+        if (!values || !valid_fft_size(n)) return false;
+        return fft_entry(values, n, nullptr, inverse, true);
+    } catch (...) {
+        return false;
+    }
+}
+
+bool blst_p1_fft_with_domain(blst_p1* values, size_t n, const blst_fr* domain, size_t domain_len, bool inverse)
+{
+    try {
+        if (!values || !domain_tag_ok(n, domain, domain_len)) return false;
+        return fft_entry(values, n, domain, inverse, true);
+    } catch (...) {
+        return false;
+    }
+}
+
+bool blst_p1_ifft_unscaled_with_domain(blst_p1* values, size_t n, const blst_fr* domain, size_t domain_len)
+{
+    try {
+        if (!values || !domain_tag_ok(n, domain, domain_len)) return false;
+        return fft_entry(values, n, domain, true, false);
+    } catch (...) {
+        return false;
+    }
+}
+
+int catmsm_p1s_mult_pippenger_device(blst_p1* ret, const void* d_points, const void* d_scalars, size_t stride,
+                                     size_t npoints, size_t nbits, size_t window)
+{
+    if (!ret) return (int)cudaErrorInvalidValue;
+    write_inf(ret);
+    if (npoints == 0 || nbits == 0) return 0;
+    if (!d_points || !d_scalars || nbits > 256 || stride < (nbits + 7) / 8 || window > 24) return (int)cudaErrorInvalidValue;
+    Ctx* ctx = get_ctx();
+    if (!ctx) return (int)cudaErrorInitializationError;
+    uint64_t out[18];
+    cudaError_t err = msm_device(ctx, d_points, (const uint8_t*)d_scalars, (uint32_t)stride, npoints,
+                                 (uint32_t)nbits, (uint32_t)window, out);
+    if (err != cudaSuccess) return (int)err;
+    std::memcpy(ret, out, sizeof(*ret));
+    return 0;
+}
+
+int catmsm_p1_fft_device(void* d_values, size_t n, const void* d_domain, int mode)
+{
+    if (!d_values || !d_domain || !valid_fft_size(n) || mode < 0 || mode > 2) return (int)cudaErrorInvalidValue;
+    Ctx* ctx = get_ctx();
+    if (!ctx) return (int)cudaErrorInitializationError;
+    const uint32_t* dr = (const uint32_t*)d_domain;
+    cudaError_t err = fft_run(ctx, d_values, n, dr, mode != 0, mode == 1 ? dr + 8 * n : nullptr);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(ctx->stream);
+    return (int)err;
+}
+
+void* catmsm_stream(void)
+{
+    Ctx* ctx = get_ctx();
+    return ctx ? (void*)ctx->stream : nullptr;
+}
+
+long catmsm_launch_count(void) { return g_stats.launches; }
+
+size_t catmsm_msm_window(size_t npoints) { return msm_default_window(npoints); }
+
+int catmsm_p1_affines_from_scalars_device(void* d_out, const void* d_k32, size_t n)
+{
+    Ctx* ctx = get_ctx();
+    if (!ctx) return (int)cudaErrorInitializationError;
+    cudaError_t err = points_from_scalars_device(ctx, (const uint8_t*)d_k32, n, d_out);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(ctx->stream);
+    return (int)err;
+}
+
+int catmsm_p1_affines_from_scalars(blst_p1_affine* out, const blst_byte* k32, size_t n)
+{
+    if (n == 0) return 0;
+    if (!out || !k32) return (int)cudaErrorInvalidValue;
+    Ctx* ctx = get_ctx();
+    if (!ctx) return (int)cudaErrorInitializationError;
+    void* dk = ctx->msm.scalars.get(32 * n);
+    void* dp = ctx->msm.points.get(sizeof(blst_p1_affine) * n);
+    if (!dk || !dp) return (int)cudaErrorMemoryAllocation;
+    cudaError_t err = cudaMemcpyAsync(dk, k32, 32 * n, cudaMemcpyHostToDevice, ctx->stream);
+    if (err == cudaSuccess) err = points_from_scalars_device(ctx, (const uint8_t*)dk, n, dp);
+    if (err == cudaSuccess)
+        err = cudaMemcpyAsync(out, dp, sizeof(blst_p1_affine) * n, cudaMemcpyDeviceToHost, ctx->stream);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(ctx->stream);
+    return (int)err;
+}
+
+int catmsm_fp_mul(blst_fp* out, const blst_fp* a, const blst_fp* b, size_t n)
+{
+    if (n == 0) return 0;
+    Ctx* ctx = get_ctx();
+    if (!ctx) return (int)cudaErrorInitializationError;
+    uint64_t* d = (uint64_t*)ctx->msm.digits.get(3 * n * sizeof(blst_fp));
+    if (!d) return (int)cudaErrorMemoryAllocation;
+    cudaError_t err = cudaMemcpyAsync(d, a, n * sizeof(blst_fp), cudaMemcpyHostToDevice, ctx->stream);
+    if (err == cudaSuccess) err = cudaMemcpyAsync(d + 6 * n, b, n * sizeof(blst_fp), cudaMemcpyHostToDevice, ctx->stream);
+    if (err == cudaSuccess) err = fp_mul_test_device(ctx, d, d + 6 * n, d + 12 * n, n);
+    if (err == cudaSuccess)
+        err = cudaMemcpyAsync(out, d + 12 * n, n * sizeof(blst_fp), cudaMemcpyDeviceToHost, ctx->stream);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(ctx->stream);
+    return (int)err;
+}
+
+}  // extern "C"

@@ -1,0 +1,26 @@
+// Internal declarations shared by the library's translation units.
+#pragma once
+#include "common.cuh"
+
+namespace catmsm {
+
+uint32_t msm_default_window(size_t n);
+
+cudaError_t msm_device(Ctx* ctx, const void* d_points, const uint8_t* d_scalars, uint32_t stride,
+                       size_t n, uint32_t nbits, uint32_t c, uint64_t* out);
+
+cudaError_t points_from_scalars_device(Ctx* ctx, const uint8_t* d_k32, size_t n, void* d_out);
+
+cudaError_t fp_mul_test_device(Ctx* ctx, const uint64_t* d_a, const uint64_t* d_b, uint64_t* d_out, size_t n);
+
+// G1 FFT over device-resident Jacobian values (blst_p1 layout).
+// d_roots_mont: the n Montgomery-form Fr roots the butterflies index;
+// inv_from_fwd: read index n - j*(n/len) (inverse from forward roots);
+// d_scale_mont: optional Montgomery-form Fr applied to every output.
+cudaError_t fft_run(Ctx* ctx, void* d_values, size_t n, const uint32_t* d_roots_mont, bool inv_from_fwd,
+                    const uint32_t* d_scale_mont);
+
+// d_out[i] = w^i (Montgomery), i < n
+cudaError_t fft_root_powers(Ctx* ctx, const uint32_t* d_w_mont, size_t n, uint32_t* d_out);
+
+}  // namespace catmsm

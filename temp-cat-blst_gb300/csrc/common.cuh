@@ -1,0 +1,99 @@
+// Shared host/device plumbing for the sm_103a BLS12-381 G1 library:
+// per-thread CUDA context (stream, grow-only device and pinned buffers) and
+// error helpers.  All public entry points are synchronous and fail closed.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstddef>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <vector>
+
+namespace catmsm {
+
+// Number of SMs on a GB300 die pair; grids are sized in multiples of it.
+constexpr int kSMs = 152;
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t cap = 0;
+    void* get(size_t bytes)
+    {
+        if (bytes == 0) bytes = 256;
+        if (bytes > cap) {
+            if (p) cudaFree(p);
+            p = nullptr;
+            cap = 0;
+            if (cudaMalloc(&p, bytes) != cudaSuccess) {
+                p = nullptr;
+                return nullptr;
+            }
+            cap = bytes;
+        }
+        return p;
+    }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+};
+
+struct PinnedBuf {
+    void* p = nullptr;
+    size_t cap = 0;
+    void* get(size_t bytes)
+    {
+        if (bytes == 0) bytes = 256;
+        if (bytes > cap) {
+            if (p) cudaFreeHost(p);
+            p = nullptr;
+            cap = 0;
+            if (cudaHostAlloc(&p, bytes, cudaHostAllocDefault) != cudaSuccess) {
+                p = nullptr;
+                return nullptr;
+            }
+            cap = bytes;
+        }
+        return p;
+    }
+};
+
+// Device workspaces of one MSM pipeline instance.
+struct MsmWork {
+    DevBuf points, scalars, digits, ranks, counts, offsets, block_sums, sorted_pt, sorted_key,
+        buckets, head, tail, seg, wins, total, status;
+};
+
+struct FftWork {
+    DevBuf values, roots, glv, scratch;
+};
+
+struct Ctx {
+    int device = -1;
+    cudaStream_t stream = nullptr;
+    MsmWork msm;
+    FftWork fft;
+    PinnedBuf h_points, h_scalars, h_out, h_values;
+    cudaEvent_t ev_a = nullptr, ev_b = nullptr;
+};
+
+// Per-thread context bound to the thread's current device.
+Ctx* get_ctx();
+
+// Launch-time stats, readable through catmsm_last_launches() for the bench.
+struct LaunchStats {
+    int launches = 0;
+};
+extern thread_local LaunchStats g_stats;
+
+#define CATMSM_CHECK(x)                    \
+    do {                                   \
+        cudaError_t e__ = (x);             \
+        if (e__ != cudaSuccess) return e__; \
+    } while (0)
+
+inline unsigned div_up(size_t a, size_t b) { return (unsigned)((a + b - 1) / b); }
+
+}  // namespace catmsm

@@ -1,0 +1,331 @@
+// G1 point arithmetic on sm_103a (y^2 = x^3 + 4 over Fp).
+//
+// Representations:
+//   affine  {x, y}            96 B, all-zero = infinity (blst_p1_affine,
+//                             bindings/blst_types.h:101)
+//   jacobian{x, y, z}         144 B, z == 0 = infinity (blst_p1, :99)
+//   xyzz    {x, y, zz, zzz}   x = X/ZZ, y = Y/ZZZ, ZZ^3 = ZZZ^2; zz == 0 =
+//                             infinity.  Same coordinates the reference uses
+//                             for its Pippenger buckets (scalar/curve/point.cpp
+//                             :1939-2113).
+// Formulas are the public explicit-formulas-database ones for a = 0:
+//   xyzz madd-2008-s / mdbl-2008-s / add-2008-s / dbl-2008-s,
+//   jacobian dbl-2009-l and add-2007-bl (with explicit special cases).
+// Every addition handles infinity, doubling and opposite inputs, so the group
+// law is complete and results are exact for any points on the curve.
+#pragma once
+#include "field.cuh"
+
+namespace catmsm {
+
+struct affine { fp x, y; };
+struct jac { fp x, y, z; };
+struct xyzz { fp x, y, zz, zzz; };
+
+__device__ __forceinline__ bool aff_is_inf(const affine& a)
+{
+    return fp_is_zero_raw(a.x) && fp_is_zero_raw(a.y);
+}
+
+__device__ __forceinline__ void xyzz_set_inf(xyzz& p)
+{
+    fp_zero(p.x); fp_zero(p.y); fp_zero(p.zz); fp_zero(p.zzz);
+}
+
+__device__ __forceinline__ bool xyzz_is_inf(const xyzz& p) { return fp_is_zero(p.zz); }
+
+// p = 2 * (ax, ay) for an affine point (mdbl-2008-s)
+__device__ __forceinline__ void xyzz_dbl_affine(xyzz& p, const fp& ax, const fp& ay)
+{
+    fp U, V, W, S, M, t;
+    fp_dbl(U, ay);
+    fp_sqr(V, U);
+    fp_mul(W, V, U);
+    fp_mul(S, ax, V);
+    fp_sqr(M, ax);
+    fp_dbl(t, M);
+    fp_add(M, t, M);
+    fp_sqr(t, M);
+    fp_sub(t, t, S);
+    fp_sub(p.x, t, S);
+    fp_sub(t, S, p.x);
+    fp_mul(t, M, t);
+    fp_mul(S, W, ay);
+    fp_sub(p.y, t, S);
+    p.zz = V;
+    p.zzz = W;
+}
+
+// p += (ax, +/-ay)   (madd-2008-s, 8M + 2S); ay already carries the sign
+__device__ __forceinline__ void xyzz_madd(xyzz& p, const fp& ax, const fp& ay)
+{
+    if (xyzz_is_inf(p)) {
+        p.x = ax; p.y = ay;
+        fp_set_one(p.zz); fp_set_one(p.zzz);
+        return;
+    }
+    fp P, R;
+    fp_mul(P, ax, p.zz);
+    fp_sub(P, P, p.x);
+    fp_mul(R, ay, p.zzz);
+    fp_sub(R, R, p.y);
+    if (fp_is_zero(P)) {
+        if (fp_is_zero(R)) xyzz_dbl_affine(p, ax, ay);
+        else xyzz_set_inf(p);
+        return;
+    }
+    fp PP, PPP, Q;
+    fp_sqr(PP, P);
+    fp_mul(PPP, PP, P);
+    fp_mul(p.zz, p.zz, PP);
+    fp_mul(p.zzz, p.zzz, PPP);
+    fp_mul(Q, p.x, PP);
+    fp_sqr(P, R);                 // P := R^2
+    fp_sub(P, P, PPP);
+    fp_sub(P, P, Q);
+    fp_sub(p.x, P, Q);            // X3 = R^2 - PPP - 2Q
+    fp_sub(Q, Q, p.x);
+    fp_mul(Q, Q, R);              // R (Q - X3)
+    fp_mul(PPP, p.y, PPP);        // Y1 PPP
+    fp_sub(p.y, Q, PPP);
+}
+
+// p = 2p (dbl-2008-s)
+__device__ __forceinline__ void xyzz_dbl(xyzz& p)
+{
+    if (xyzz_is_inf(p)) return;
+    fp U, V, W, S, M, t;
+    fp_dbl(U, p.y);
+    fp_sqr(V, U);
+    fp_mul(W, V, U);
+    fp_mul(S, p.x, V);
+    fp_sqr(M, p.x);
+    fp_dbl(t, M);
+    fp_add(M, t, M);
+    fp_mul(p.zz, p.zz, V);
+    fp_mul(p.zzz, p.zzz, W);
+    fp_sqr(t, M);
+    fp_sub(t, t, S);
+    fp_sub(p.x, t, S);
+    fp_sub(t, S, p.x);
+    fp_mul(t, M, t);
+    fp_mul(W, W, p.y);
+    fp_sub(p.y, t, W);
+}
+
+// p += q (add-2008-s, 12M + 2S)
+__device__ __forceinline__ void xyzz_add(xyzz& p, const xyzz& q)
+{
+    if (xyzz_is_inf(q)) return;
+    if (xyzz_is_inf(p)) { p = q; return; }
+    fp U1, S1, P, R;
+    fp_mul(U1, p.x, q.zz);
+    fp_mul(P, q.x, p.zz);
+    fp_sub(P, P, U1);
+    fp_mul(S1, p.y, q.zzz);
+    fp_mul(R, q.y, p.zzz);
+    fp_sub(R, R, S1);
+    if (fp_is_zero(P)) {
+        if (fp_is_zero(R)) xyzz_dbl(p);
+        else xyzz_set_inf(p);
+        return;
+    }
+    fp PP, PPP;
+    fp_sqr(PP, P);
+    fp_mul(PPP, PP, P);
+    fp_mul(p.zz, p.zz, q.zz);
+    fp_mul(p.zz, p.zz, PP);
+    fp_mul(p.zzz, p.zzz, q.zzz);
+    fp_mul(p.zzz, p.zzz, PPP);
+    fp_mul(U1, U1, PP);           // Q = U1 PP
+    fp_sqr(P, R);
+    fp_sub(P, P, PPP);
+    fp_sub(P, P, U1);
+    fp_sub(p.x, P, U1);
+    fp_sub(U1, U1, p.x);
+    fp_mul(U1, U1, R);
+    fp_mul(S1, S1, PPP);
+    fp_sub(p.y, U1, S1);
+}
+
+__device__ __forceinline__ void xyzz_neg(xyzz& p) { fp_neg(p.y, p.y); }
+
+// Jacobian (X, Y, Z) = (x*zz, y*zzz, zz); reference point.cpp:2109
+__device__ __forceinline__ void xyzz_to_jac(jac& o, const xyzz& p)
+{
+    if (xyzz_is_inf(p)) {
+        fp_zero(o.x); fp_zero(o.y); fp_zero(o.z);
+        return;
+    }
+    fp_mul(o.x, p.x, p.zz);
+    fp_mul(o.y, p.y, p.zzz);
+    o.z = p.zz;
+}
+
+// xyzz from Jacobian: zz = Z^2, zzz = Z^3
+__device__ __forceinline__ void jac_to_xyzz(xyzz& o, const jac& p)
+{
+    if (fp_is_zero(p.z)) { xyzz_set_inf(o); return; }
+    o.x = p.x;
+    o.y = p.y;
+    fp_sqr(o.zz, p.z);
+    fp_mul(o.zzz, o.zz, p.z);
+}
+
+// Affine normalisation of an xyzz point: x = X / ZZ, y = Y / ZZZ.
+// 1/ZZ and 1/ZZZ come from one inversion of ZZZ*ZZ... via (ZZ*ZZZ)^-1.
+__device__ __forceinline__ void xyzz_to_affine(affine& o, const xyzz& p)
+{
+    if (xyzz_is_inf(p)) { fp_zero(o.x); fp_zero(o.y); return; }
+    fp t, inv;
+    fp_mul(t, p.zz, p.zzz);
+    fp_inv(inv, t);
+    fp_mul(t, inv, p.zzz);        // 1/ZZ
+    fp_mul(o.x, p.x, t);
+    fp_mul(t, inv, p.zz);         // 1/ZZZ
+    fp_mul(o.y, p.y, t);
+    fp_canon(o.x, o.x);
+    fp_canon(o.y, o.y);
+}
+
+
+// ---------------------------------------------------------------- Jacobian
+__device__ __forceinline__ bool jac_is_inf(const jac& p) { return fp_is_zero(p.z); }
+
+__device__ __forceinline__ void jac_set_inf(jac& p) { fp_zero(p.x); fp_zero(p.y); fp_zero(p.z); }
+
+// dbl-2009-l (a = 0): 2M + 5S
+__device__ __forceinline__ void jac_dbl(jac& p)
+{
+    if (jac_is_inf(p)) return;
+    fp A, B, C, D, E, t;
+    fp_sqr(A, p.x);
+    fp_sqr(B, p.y);
+    fp_sqr(C, B);
+    fp_add(t, p.x, B);
+    fp_sqr(t, t);
+    fp_sub(t, t, A);
+    fp_sub(t, t, C);
+    fp_dbl(D, t);
+    fp_dbl(E, A);
+    fp_add(E, E, A);
+    fp_mul(p.z, p.y, p.z);
+    fp_dbl(p.z, p.z);
+    fp_sqr(t, E);
+    fp_sub(t, t, D);
+    fp_sub(p.x, t, D);
+    fp_sub(t, D, p.x);
+    fp_mul(t, E, t);
+    fp_dbl(C, C);
+    fp_dbl(C, C);
+    fp_dbl(C, C);
+    fp_sub(p.y, t, C);
+}
+
+// p += q, add-2007-bl style with explicit infinity / doubling / opposite cases
+__device__ __forceinline__ void jac_add(jac& p, const jac& q)
+{
+    if (jac_is_inf(q)) return;
+    if (jac_is_inf(p)) { p = q; return; }
+    fp z1z1, z2z2, u1, h, s1, r, t;
+    fp_sqr(z1z1, p.z);
+    fp_sqr(z2z2, q.z);
+    fp_mul(u1, p.x, z2z2);
+    fp_mul(h, q.x, z1z1);
+    fp_sub(h, h, u1);
+    fp_mul(s1, p.y, q.z);
+    fp_mul(s1, s1, z2z2);
+    fp_mul(r, q.y, p.z);
+    fp_mul(r, r, z1z1);
+    fp_sub(r, r, s1);
+    if (fp_is_zero(h)) {
+        if (fp_is_zero(r)) jac_dbl(p);
+        else jac_set_inf(p);
+        return;
+    }
+    fp_mul(p.z, p.z, q.z);
+    fp_mul(p.z, p.z, h);
+    fp_sqr(t, h);                 // HH
+    fp_mul(u1, u1, t);            // V = U1 HH
+    fp_mul(t, t, h);              // HHH
+    fp_mul(s1, s1, t);            // S1 HHH
+    fp_sqr(z1z1, r);
+    fp_sub(z1z1, z1z1, t);
+    fp_sub(z1z1, z1z1, u1);
+    fp_sub(p.x, z1z1, u1);        // X3 = R^2 - HHH - 2V
+    fp_sub(u1, u1, p.x);
+    fp_mul(u1, u1, r);
+    fp_sub(p.y, u1, s1);          // Y3 = R (V - X3) - S1 HHH
+}
+
+__device__ __forceinline__ void jac_neg(jac& p) { fp_neg(p.y, p.y); }
+
+// GLV endomorphism of G1: phi(x, y) = (beta x, y) = lambda (x, y) for
+// lambda = z^2 - 1 = 0xac45a4010001a40200000000ffffffff (lambda^2 + lambda + 1 = r)
+// and the cube root of unity beta below (Montgomery form).
+__device__ __constant__ static const uint32_t FP_BETA[12] = {
+    0x8671f071u, 0xcd03c9e4u, 0x1fcda5d2u, 0x5dab2246u, 0xd3851b95u, 0x587042afu,
+    0x01bacb9eu, 0x8eb60ebeu, 0x83d050d2u, 0x03f97d6eu, 0x54638741u, 0x18f02065u};
+
+// width-5 NAF digits of a 128-bit value (4 little-endian words); returns length
+__device__ __forceinline__ int wnaf5_128(int8_t* d, const uint32_t* kin)
+{
+    uint32_t k[5] = {kin[0], kin[1], kin[2], kin[3], 0};
+    int len = 0;
+    while ((k[0] | k[1] | k[2] | k[3] | k[4]) != 0) {
+        int v = 0;
+        if (k[0] & 1) {
+            v = (int)(k[0] & 31);
+            if (v >= 16) v -= 32;
+            if (v > 0) {
+                uint32_t b = (uint32_t)v;
+                for (int i = 0; i < 5 && b; i++) { uint32_t o = k[i]; k[i] -= b; b = o < b; }
+            } else {
+                uint32_t cy = (uint32_t)(-v);
+                for (int i = 0; i < 5 && cy; i++) { k[i] += cy; cy = k[i] < cy; }
+            }
+        }
+        d[len++] = (int8_t)v;
+        for (int i = 0; i < 4; i++) k[i] = (k[i] >> 1) | (k[i + 1] << 31);
+        k[4] >>= 1;
+    }
+    return len;
+}
+
+// out = (k1 + lambda k2) P for 128-bit k1, k2 (GLV + interleaved wNAF-5).
+// P must be in the prime-order subgroup (as the FFT contract requires).
+static __device__ __noinline__ void jac_mult_glv(jac& out, const jac& P, const uint32_t* k1, const uint32_t* k2)
+{
+    int8_t d1[132], d2[132];
+    const int l1 = wnaf5_128(d1, k1);
+    const int l2 = wnaf5_128(d2, k2);
+    jac T[8];
+    T[0] = P;
+    jac P2 = P;
+    jac_dbl(P2);
+    for (int i = 1; i < 8; i++) { T[i] = T[i - 1]; jac_add(T[i], P2); }
+    fp beta;
+#pragma unroll
+    for (int i = 0; i < 12; i++) beta.v[i] = FP_BETA[i];
+    jac acc;
+    jac_set_inf(acc);
+    for (int i = (l1 > l2 ? l1 : l2) - 1; i >= 0; i--) {
+        jac_dbl(acc);
+        const int a = i < l1 ? d1[i] : 0;
+        const int b = i < l2 ? d2[i] : 0;
+        if (a) {
+            jac t = T[(a > 0 ? a : -a) >> 1];
+            if (a < 0) jac_neg(t);
+            jac_add(acc, t);
+        }
+        if (b) {
+            jac t = T[(b > 0 ? b : -b) >> 1];
+            fp_mul(t.x, t.x, beta);
+            if (b < 0) jac_neg(t);
+            jac_add(acc, t);
+        }
+    }
+    out = acc;
+}
+
+}  // namespace catmsm

@@ -1,0 +1,116 @@
+// BLS12-381 scalar field Fr on device: 8 x 32-bit limbs, Montgomery form with
+// R = 2^256 (same bytes as the reference's 4 x u64 blst_fr, scalar/fields/
+// Fr.h:44-125).  Used only to prepare FFT roots (powers, from_mont, GLV split),
+// which is O(n) work next to O(n log n) group operations, so a plain CIOS with
+// 64-bit accumulators suffices here.
+#pragma once
+#include <cstdint>
+
+namespace catmsm {
+
+__device__ __constant__ static const uint32_t FR_R[8] = {
+    0x00000001u, 0xffffffffu, 0xfffe5bfeu, 0x53bda402u, 0x09a1d805u, 0x3339d808u, 0x299d7d48u, 0x73eda753u};
+__device__ __constant__ static const uint32_t FR_ONE_MONT[8] = {
+    // 2^256 mod r
+    0xfffffffeu, 0x00000001u, 0x00034802u, 0x5884b7fau, 0xecbc4ff5u, 0x998c4fefu, 0xacc5056fu, 0x1824b159u};
+constexpr uint32_t FR_N0 = 0xffffffffu;
+// lambda = 0xac45a4010001a40200000000ffffffff (GLV eigenvalue, lambda^2 + lambda + 1 = r)
+__device__ __constant__ static const uint32_t FR_LAMBDA[4] = {0xffffffffu, 0x00000000u, 0x0001a402u, 0xac45a401u};
+
+__device__ __forceinline__ bool fr_geq(const uint32_t* a, const uint32_t* b)
+{
+    for (int i = 7; i >= 0; i--)
+        if (a[i] != b[i]) return a[i] > b[i];
+    return true;
+}
+
+__device__ __forceinline__ void fr_sub_r(uint32_t* a)
+{
+    uint64_t br = 0;
+    for (int i = 0; i < 8; i++) {
+        uint64_t d = (uint64_t)a[i] - FR_R[i] - br;
+        a[i] = (uint32_t)d;
+        br = (d >> 63) & 1;
+    }
+}
+
+// o = a * b * 2^-256 mod r (reduced)
+__device__ __forceinline__ void fr_mul(uint32_t* o, const uint32_t* a, const uint32_t* b)
+{
+    uint32_t t[10];
+    for (int i = 0; i < 10; i++) t[i] = 0;
+    for (int i = 0; i < 8; i++) {
+        uint64_t c = 0;
+        for (int j = 0; j < 8; j++) {
+            c += (uint64_t)a[j] * b[i] + t[j];
+            t[j] = (uint32_t)c;
+            c >>= 32;
+        }
+        c += t[8];
+        t[8] = (uint32_t)c;
+        t[9] = (uint32_t)(c >> 32);
+        const uint32_t m = t[0] * FR_N0;
+        c = ((uint64_t)m * FR_R[0] + t[0]) >> 32;
+        for (int j = 1; j < 8; j++) {
+            c += (uint64_t)m * FR_R[j] + t[j];
+            t[j - 1] = (uint32_t)c;
+            c >>= 32;
+        }
+        c += t[8];
+        t[7] = (uint32_t)c;
+        t[8] = t[9] + (uint32_t)(c >> 32);
+    }
+    if (t[8] || fr_geq(t, FR_R)) fr_sub_r(t);
+    for (int i = 0; i < 8; i++) o[i] = t[i];
+}
+
+__device__ __forceinline__ void fr_from_mont(uint32_t* o, const uint32_t* a)
+{
+    const uint32_t one[8] = {1, 0, 0, 0, 0, 0, 0, 0};
+    fr_mul(o, a, one);
+}
+
+// o = base^e (Montgomery in/out), e < 2^32
+__device__ __forceinline__ void fr_pow_u32(uint32_t* o, const uint32_t* base, uint32_t e)
+{
+    uint32_t acc[8], b[8];
+    for (int i = 0; i < 8; i++) { acc[i] = FR_ONE_MONT[i]; b[i] = base[i]; }
+    while (e) {
+        if (e & 1) fr_mul(acc, acc, b);
+        fr_mul(b, b, b);
+        e >>= 1;
+    }
+    for (int i = 0; i < 8; i++) o[i] = acc[i];
+}
+
+// GLV split of a canonical k < r: k = k1 + lambda * k2, 0 <= k1 < lambda, k2 <= lambda + 1
+// (binary long division; both halves fit 128 bits).
+__device__ __forceinline__ void fr_glv_split(uint32_t* k1, uint32_t* k2, const uint32_t* k)
+{
+    uint32_t rem[5] = {0, 0, 0, 0, 0};
+    uint32_t q[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int i = 255; i >= 0; i--) {
+        for (int w = 4; w > 0; w--) rem[w] = (rem[w] << 1) | (rem[w - 1] >> 31);
+        rem[0] = (rem[0] << 1) | ((k[i >> 5] >> (i & 31)) & 1);
+        bool ge = rem[4] != 0;
+        if (!ge) {
+            ge = true;
+            for (int w = 3; w >= 0; w--) {
+                if (rem[w] != FR_LAMBDA[w]) { ge = rem[w] > FR_LAMBDA[w]; break; }
+            }
+        }
+        if (ge) {
+            uint64_t br = 0;
+            for (int w = 0; w < 4; w++) {
+                uint64_t d = (uint64_t)rem[w] - FR_LAMBDA[w] - br;
+                rem[w] = (uint32_t)d;
+                br = (d >> 63) & 1;
+            }
+            rem[4] -= (uint32_t)br;
+            q[i >> 5] |= 1u << (i & 31);
+        }
+    }
+    for (int w = 0; w < 4; w++) { k1[w] = rem[w]; k2[w] = q[w]; }
+}
+
+}  // namespace catmsm

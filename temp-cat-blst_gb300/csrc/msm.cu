@@ -1,0 +1,437 @@
+// BLS12-381 G1 Pippenger MSM on sm_103a.
+//
+// Drop-in for blst_p1s_mult_pippenger (reference c_api.cpp:1382-1418,
+// multi_scalar.cpp:806-923).  The result is the same group element
+// sum_i (k_i mod 2^nbits) * P_i; the device pipeline is:
+//
+//   1. k_digits      signed c-bit window digits (carry recoding, digit in
+//                    [-2^(c-1), 2^(c-1)]), one thread per scalar; each nonzero
+//                    digit takes a rank in its bucket with one atomicAdd.
+//   2. k_scan_*      exclusive scan of the D * 2^(c-1) bucket counts.
+//   3. k_scatter     counting-sort scatter of (point index | sign) into bucket
+//                    order, plus each entry's bucket key.
+//   4. k_accumulate  load-balanced bucket accumulation: every thread owns a
+//                    fixed chunk of L sorted entries and folds runs of equal
+//                    keys with XYZZ mixed adds; runs that cross a chunk edge
+//                    go to head/tail carry slots.
+//   5. k_fixup       joins carry slots of buckets that span chunks.
+//   6. k_reduce_seg  running-sum reduction sum_d d * S_d over segments of S
+//                    buckets, plus (segment offset) * (segment sum).
+//   7. k_reduce_win  block tree-sum of the segments of each window.
+//   8. host          folds the D window sums: ret = 2^c ret + W_w, top first
+//                    (reference multi_scalar.cpp:913-922), then normalises.
+#include "common.cuh"
+#include "curve.cuh"
+#include "host_curve.hpp"
+#include "catmsm_internal.h"
+
+#include <mutex>
+
+namespace catmsm {
+
+thread_local LaunchStats g_stats;
+
+// ----------------------------------------------------------------- loads/stores
+__device__ __forceinline__ void load_affine(fp& x, fp& y, const affine* p)
+{
+    const uint4* q = reinterpret_cast<const uint4*>(p);
+    uint4 v[6];
+#pragma unroll
+    for (int k = 0; k < 6; k++) v[k] = __ldg(q + k);
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        x.v[4 * k + 0] = v[k].x; x.v[4 * k + 1] = v[k].y;
+        x.v[4 * k + 2] = v[k].z; x.v[4 * k + 3] = v[k].w;
+        y.v[4 * k + 0] = v[k + 3].x; y.v[4 * k + 1] = v[k + 3].y;
+        y.v[4 * k + 2] = v[k + 3].z; y.v[4 * k + 3] = v[k + 3].w;
+    }
+}
+
+__device__ __forceinline__ void store_xyzz(xyzz* dst, const xyzz& p)
+{
+    uint4* q = reinterpret_cast<uint4*>(dst);
+    const uint32_t* s = reinterpret_cast<const uint32_t*>(&p);
+#pragma unroll
+    for (int k = 0; k < 12; k++) q[k] = make_uint4(s[4 * k], s[4 * k + 1], s[4 * k + 2], s[4 * k + 3]);
+}
+
+__device__ __forceinline__ void load_xyzz(xyzz& p, const xyzz* src)
+{
+    const uint4* q = reinterpret_cast<const uint4*>(src);
+    uint32_t* d = reinterpret_cast<uint32_t*>(&p);
+#pragma unroll
+    for (int k = 0; k < 12; k++) {
+        uint4 v = q[k];
+        d[4 * k] = v.x; d[4 * k + 1] = v.y; d[4 * k + 2] = v.z; d[4 * k + 3] = v.w;
+    }
+}
+
+// ----------------------------------------------------------------- 1. digits
+__global__ void k_digits(const uint8_t* __restrict__ scalars, uint32_t stride, uint32_t n,
+                         uint32_t nbits, uint32_t c, uint32_t D, uint32_t* __restrict__ digits,
+                         uint32_t* __restrict__ ranks, uint32_t* __restrict__ counts)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t k[9];
+#pragma unroll
+    for (int j = 0; j < 9; j++) k[j] = 0;
+    const uint8_t* s = scalars + (size_t)i * stride;
+    const uint32_t nbytes = (nbits + 7) >> 3;
+    if (stride == 32 && (reinterpret_cast<uintptr_t>(s) & 15) == 0) {
+        const uint4 a = __ldg(reinterpret_cast<const uint4*>(s));
+        const uint4 b = __ldg(reinterpret_cast<const uint4*>(s) + 1);
+        k[0] = a.x; k[1] = a.y; k[2] = a.z; k[3] = a.w;
+        k[4] = b.x; k[5] = b.y; k[6] = b.z; k[7] = b.w;
+    } else {
+        for (uint32_t b = 0; b < nbytes; b++) k[b >> 2] |= (uint32_t)s[b] << (8 * (b & 3));
+    }
+#pragma unroll
+    for (uint32_t j = 0; j < 8; j++) {
+        if (nbits <= 32 * j) k[j] = 0;
+        else if (nbits < 32 * (j + 1)) k[j] &= (1u << (nbits - 32 * j)) - 1;
+    }
+    const uint32_t B = 1u << (c - 1);
+    const uint32_t cmask = (1u << c) - 1;
+    uint32_t carry = 0;
+    for (uint32_t w = 0; w < D; w++) {
+        const uint32_t bit = w * c, word = bit >> 5, sh = bit & 31;
+        uint32_t raw = k[word] >> sh;
+        if (sh && word + 1 < 9) raw |= k[word + 1] << (32 - sh);
+        raw &= cmask;
+        int32_t d = (int32_t)(raw + carry);
+        if (d > (int32_t)B) { d -= (int32_t)(cmask + 1); carry = 1; }
+        else carry = 0;
+        const size_t o = (size_t)w * n + i;
+        if (d == 0) {
+            digits[o] = 0xffffffffu;
+        } else {
+            const uint32_t mag = d < 0 ? (uint32_t)(-d) : (uint32_t)d;
+            const uint32_t key = w * B + (mag - 1);
+            ranks[o] = atomicAdd(&counts[key], 1u);
+            digits[o] = key | (d < 0 ? 0x80000000u : 0u);
+        }
+    }
+}
+
+// ----------------------------------------------------------------- 2. scan
+constexpr int kScanThreads = 1024;
+constexpr int kScanPer = 4;
+constexpr int kScanTile = kScanThreads * kScanPer;
+
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* smem_warp, uint32_t* total)
+{
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, x, d);
+        if (lane >= d) x += y;
+    }
+    if (lane == 31) smem_warp[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        const int nw = blockDim.x >> 5;
+        uint32_t t = lane < nw ? smem_warp[lane] : 0;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, t, d);
+            if (lane >= d) t += y;
+        }
+        if (lane < nw) smem_warp[lane] = t;
+    }
+    __syncthreads();
+    const uint32_t warp_prefix = wid ? smem_warp[wid - 1] : 0;
+    *total = smem_warp[(blockDim.x >> 5) - 1];
+    return warp_prefix + x - v;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_local(const uint32_t* __restrict__ in,
+                                                              uint32_t* __restrict__ out,
+                                                              uint32_t* __restrict__ block_sums, uint32_t M)
+{
+    __shared__ uint32_t sw[32];
+    const size_t base = (size_t)blockIdx.x * kScanTile + (size_t)threadIdx.x * kScanPer;
+    uint32_t v[kScanPer], s = 0;
+#pragma unroll
+    for (int j = 0; j < kScanPer; j++) {
+        v[j] = base + j < M ? in[base + j] : 0;
+        s += v[j];
+    }
+    uint32_t total;
+    uint32_t pre = block_exclusive_scan(s, sw, &total);
+#pragma unroll
+    for (int j = 0; j < kScanPer; j++) {
+        if (base + j < M) out[base + j] = pre;
+        pre += v[j];
+    }
+    if (threadIdx.x == 0) block_sums[blockIdx.x] = total;
+}
+
+// Single block: exclusive scan of the block sums; writes grand total to *total_out.
+__global__ void __launch_bounds__(kScanThreads) k_scan_top(uint32_t* __restrict__ block_sums, uint32_t nb,
+                                                            uint32_t* __restrict__ total_out)
+{
+    __shared__ uint32_t sw[32];
+    const uint32_t per = (nb + kScanThreads - 1) / kScanThreads;
+    const uint32_t b0 = threadIdx.x * per;
+    uint32_t s = 0;
+    for (uint32_t j = 0; j < per; j++)
+        if (b0 + j < nb) s += block_sums[b0 + j];
+    uint32_t total;
+    uint32_t pre = block_exclusive_scan(s, sw, &total);
+    for (uint32_t j = 0; j < per; j++) {
+        if (b0 + j < nb) {
+            uint32_t t = block_sums[b0 + j];
+            block_sums[b0 + j] = pre;
+            pre += t;
+        }
+    }
+    if (threadIdx.x == 0) *total_out = total;
+}
+
+__global__ void k_scan_add(uint32_t* __restrict__ out, const uint32_t* __restrict__ block_sums, uint32_t M)
+{
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < M) out[i] += block_sums[i / kScanTile];
+}
+
+// ----------------------------------------------------------------- 3. scatter
+__global__ void k_scatter(const uint32_t* __restrict__ digits, const uint32_t* __restrict__ ranks,
+                          const uint32_t* __restrict__ offsets, uint32_t n, uint32_t nD,
+                          uint32_t* __restrict__ sorted_pt, uint32_t* __restrict__ sorted_key)
+{
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= nD) return;
+    const uint32_t dg = digits[j];
+    if (dg == 0xffffffffu) return;
+    const uint32_t key = dg & 0x7fffffffu;
+    const uint32_t pos = offsets[key] + ranks[j];
+    sorted_pt[pos] = (j % n) | (dg & 0x80000000u);
+    sorted_key[pos] = key;
+}
+
+// ----------------------------------------------------------------- 4. accumulate
+__device__ __forceinline__ void madd_entry(xyzz& acc, const affine* __restrict__ pts, uint32_t v)
+{
+    fp x, y;
+    load_affine(x, y, pts + (v & 0x7fffffffu));
+    if (fp_is_zero_raw(x) && fp_is_zero_raw(y)) return;   // infinity contributes nothing
+    if (v >> 31) fp_neg(y, y);
+    xyzz_madd(acc, x, y);
+}
+
+__global__ void __launch_bounds__(128) k_accumulate(const affine* __restrict__ pts,
+                                                    const uint32_t* __restrict__ sorted_pt,
+                                                    const uint32_t* __restrict__ sorted_key,
+                                                    const uint32_t* __restrict__ total_ptr, uint32_t L,
+                                                    xyzz* __restrict__ buckets, xyzz* __restrict__ head,
+                                                    xyzz* __restrict__ tail)
+{
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t E = *total_ptr;
+    const size_t start = (size_t)t * L;
+    if (start >= E) return;
+    const uint32_t end = (uint32_t)min((size_t)E, start + L);
+    uint32_t cur = sorted_key[start];
+    const bool starts_before = start > 0 && sorted_key[start - 1] == cur;
+    bool first_run = true;
+    xyzz acc;
+    xyzz_set_inf(acc);
+    for (uint32_t e = (uint32_t)start; e < end; e++) {
+        const uint32_t key = sorted_key[e];
+        if (key != cur) {
+            if (first_run && starts_before) store_xyzz(head + t, acc);
+            else store_xyzz(buckets + cur, acc);
+            first_run = false;
+            xyzz_set_inf(acc);
+            cur = key;
+        }
+        madd_entry(acc, pts, sorted_pt[e]);
+    }
+    const bool continues_after = end < E && sorted_key[end] == cur;
+    if (first_run && starts_before) store_xyzz(head + t, acc);
+    else if (continues_after) store_xyzz(tail + t, acc);
+    else store_xyzz(buckets + cur, acc);
+}
+
+// ----------------------------------------------------------------- 5. fixup
+__global__ void __launch_bounds__(128) k_fixup(const uint32_t* __restrict__ sorted_key,
+                                               const uint32_t* __restrict__ total_ptr, uint32_t L,
+                                               xyzz* __restrict__ buckets, const xyzz* __restrict__ head,
+                                               const xyzz* __restrict__ tail)
+{
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t E = *total_ptr;
+    const size_t start = (size_t)t * L;
+    if (start >= E) return;
+    const uint32_t end = (uint32_t)min((size_t)E, start + L);
+    const uint32_t last = sorted_key[end - 1];
+    if (!(end < E && sorted_key[end] == last)) return;                 // bucket ends here
+    const bool single = sorted_key[start] == last;
+    const bool starts_before = start > 0 && sorted_key[start - 1] == sorted_key[start];
+    if (single && starts_before) return;                               // a middle chunk
+    xyzz acc, part;
+    load_xyzz(acc, tail + t);
+    for (uint32_t u = t + 1;; u++) {
+        load_xyzz(part, head + u);
+        xyzz_add(acc, part);
+        const size_t s = (size_t)u * L;
+        const uint32_t e = (uint32_t)min((size_t)E, s + L);
+        const bool u_single = sorted_key[e - 1] == last;
+        const bool u_cont = e < E && sorted_key[e] == last;
+        if (!(u_single && u_cont)) break;
+    }
+    store_xyzz(buckets + last, acc);
+}
+
+// ----------------------------------------------------------------- 6/7. reduce
+__global__ void __launch_bounds__(128) k_reduce_seg(const xyzz* __restrict__ buckets, uint32_t B,
+                                                    uint32_t S, uint32_t D, xyzz* __restrict__ seg_out)
+{
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t T = B / S;
+    if (t >= D * T) return;
+    const uint32_t w = t / T, s = t % T;
+    const xyzz* base = buckets + (size_t)w * B + (size_t)s * S;
+    xyzz acc, tri, b;
+    xyzz_set_inf(acc);
+    xyzz_set_inf(tri);
+    for (int j = (int)S - 1; j >= 0; j--) {
+        load_xyzz(b, base + j);
+        xyzz_add(acc, b);
+        xyzz_add(tri, acc);
+    }
+    // tri += (s*S) * acc : the digits of this segment start at s*S + 1
+    const uint32_t k = s * S;
+    if (k) {
+        xyzz m;
+        xyzz_set_inf(m);
+        for (int bit = 31 - __clz(k); bit >= 0; bit--) {
+            xyzz_dbl(m);
+            if ((k >> bit) & 1) xyzz_add(m, acc);
+        }
+        xyzz_add(tri, m);
+    }
+    store_xyzz(seg_out + t, tri);
+}
+
+constexpr int kWinThreads = 128;
+
+__global__ void __launch_bounds__(kWinThreads) k_reduce_win(const xyzz* __restrict__ seg, uint32_t T,
+                                                            xyzz* __restrict__ wins)
+{
+    __shared__ xyzz sh[kWinThreads];
+    const uint32_t w = blockIdx.x;
+    xyzz acc, b;
+    xyzz_set_inf(acc);
+    for (uint32_t s = threadIdx.x; s < T; s += kWinThreads) {
+        load_xyzz(b, seg + (size_t)w * T + s);
+        xyzz_add(acc, b);
+    }
+    sh[threadIdx.x] = acc;
+    __syncthreads();
+    for (int h = kWinThreads / 2; h > 0; h >>= 1) {
+        if ((int)threadIdx.x < h) {
+            xyzz a = sh[threadIdx.x];
+            xyzz_add(a, sh[threadIdx.x + h]);
+            sh[threadIdx.x] = a;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) store_xyzz(wins + w, sh[0]);
+}
+
+// ----------------------------------------------------------------- host driver
+static uint32_t ilog2(size_t n)
+{
+    uint32_t k = 0;
+    while (n >>= 1) k++;
+    return k;
+}
+
+uint32_t msm_default_window(size_t n)
+{
+    const uint32_t lg = ilog2(n);
+    int c = (int)lg - 4;
+    if (c < 4) c = 4;
+    if (c > 20) c = 20;
+    return (uint32_t)c;
+}
+
+// Runs the device pipeline over device-resident points/scalars on the context
+// stream and returns the folded, normalised result in `out` (144 bytes).
+cudaError_t msm_device(Ctx* ctx, const void* d_points, const uint8_t* d_scalars, uint32_t stride,
+                       size_t n, uint32_t nbits, uint32_t c, uint64_t* out)
+{
+    cudaStream_t st = ctx->stream;
+    MsmWork& W = ctx->msm;
+    if (c == 0) c = msm_default_window(n);
+    if (c < 2 || c > 22 || n == 0 || n > 0x7fffffffu) return cudaErrorInvalidValue;
+    const uint32_t D = nbits / c + 1;
+    const uint32_t B = 1u << (c - 1);
+    const size_t M = (size_t)D * B;
+    const size_t nD = (size_t)n * D;
+    if (nD > 0xffffffffu - 1) return cudaErrorInvalidValue;
+    uint32_t L = (uint32_t)(nD / ((size_t)kSMs * 1024));
+    if (L < 4) L = 4;
+    if (L > 64) L = 64;
+    const size_t chunks = (nD + L - 1) / L;
+    uint32_t S = 8;
+    if (S > B) S = B;
+    const uint32_t T = B / S;
+
+    uint32_t* digits = (uint32_t*)W.digits.get(nD * 4);
+    uint32_t* ranks = (uint32_t*)W.ranks.get(nD * 4);
+    uint32_t* counts = (uint32_t*)W.counts.get(M * 4);
+    uint32_t* offsets = (uint32_t*)W.offsets.get((M + 1) * 4);
+    const uint32_t nblocks = div_up(M, kScanTile);
+    uint32_t* bsums = (uint32_t*)W.block_sums.get((size_t)nblocks * 4);
+    uint32_t* sorted_pt = (uint32_t*)W.sorted_pt.get(nD * 4);
+    uint32_t* sorted_key = (uint32_t*)W.sorted_key.get(nD * 4);
+    xyzz* buckets = (xyzz*)W.buckets.get(M * sizeof(xyzz));
+    xyzz* head = (xyzz*)W.head.get(chunks * sizeof(xyzz));
+    xyzz* tail = (xyzz*)W.tail.get(chunks * sizeof(xyzz));
+    xyzz* seg = (xyzz*)W.seg.get((size_t)D * T * sizeof(xyzz));
+    xyzz* wins = (xyzz*)W.wins.get((size_t)D * sizeof(xyzz));
+    uint64_t* h_wins = (uint64_t*)ctx->h_out.get((size_t)D * sizeof(xyzz));
+    if (!digits || !ranks || !counts || !offsets || !bsums || !sorted_pt || !sorted_key || !buckets ||
+        !head || !tail || !seg || !wins || !h_wins)
+        return cudaErrorMemoryAllocation;
+    uint32_t* total = offsets + M;
+
+    CATMSM_CHECK(cudaMemsetAsync(counts, 0, M * 4, st));
+    CATMSM_CHECK(cudaMemsetAsync(buckets, 0, M * sizeof(xyzz), st));
+    k_digits<<<div_up(n, 256), 256, 0, st>>>(d_scalars, stride, (uint32_t)n, nbits, c, D, digits, ranks, counts);
+    k_scan_local<<<nblocks, kScanThreads, 0, st>>>(counts, offsets, bsums, (uint32_t)M);
+    k_scan_top<<<1, kScanThreads, 0, st>>>(bsums, nblocks, total);
+    k_scan_add<<<div_up(M, 256), 256, 0, st>>>(offsets, bsums, (uint32_t)M);
+    k_scatter<<<div_up(nD, 256), 256, 0, st>>>(digits, ranks, offsets, (uint32_t)n, (uint32_t)nD, sorted_pt,
+                                              sorted_key);
+    k_accumulate<<<div_up(chunks, 128), 128, 0, st>>>((const affine*)d_points, sorted_pt, sorted_key, total, L,
+                                                      buckets, head, tail);
+    k_fixup<<<div_up(chunks, 128), 128, 0, st>>>(sorted_key, total, L, buckets, head, tail);
+    k_reduce_seg<<<div_up((size_t)D * T, 128), 128, 0, st>>>(buckets, B, S, D, seg);
+    k_reduce_win<<<D, kWinThreads, 0, st>>>(seg, T, wins);
+    g_stats.launches += 9;
+    CATMSM_CHECK(cudaGetLastError());
+    CATMSM_CHECK(cudaMemcpyAsync(h_wins, wins, (size_t)D * sizeof(xyzz), cudaMemcpyDeviceToHost, st));
+    CATMSM_CHECK(cudaStreamSynchronize(st));
+
+    using namespace catmsm_host;
+    hjac ret;
+    std::memset(&ret, 0, sizeof(ret));
+    for (uint32_t w = D; w-- > 0;) {
+        hjac tile;
+        from_device_xyzz(tile, h_wins + (size_t)w * 24);
+        jac_add(ret, ret, tile);
+        if (w)
+            for (uint32_t i = 0; i < c; i++) jac_dbl(ret, ret);
+    }
+    hjac norm;
+    normalize(norm, ret);
+    std::memcpy(out, &norm, 144);
+    return cudaSuccess;
+}
+
+}  // namespace catmsm

@@ -1,0 +1,105 @@
+"""Regenerate tests/golden/golden.json from the REFERENCE library.
+
+Run in a tree where the reference sources are present:
+    make -C oracle ref && python tests/golden/make_golden.py [--large]
+
+Inputs are seeded (oracle.gen_* / synth.py); outputs come from the
+reference's own C ABI built from its sources (oracle/_ref/libblst_ref.so):
+  * msm:  blst_p1s_mult_pippenger -> blst_p1_compress (48 bytes, hex)
+  * fft:  blst_p1_fft / blst_p1_fft_with_domain / blst_p1_ifft_unscaled_with_domain
+          -> blst_p1_serialize of every element; small n stored in full,
+          larger n as sha256 of the concatenation
+  * domain: blst_fr_fft_domain_init bytes (sha256) per size
+"""
+import hashlib
+import json
+import os
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+from oracle import Oracle, Reference, build  # noqa: E402
+
+OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden.json")
+
+
+def msm_inputs(o, seed, n, kind, nbits, dup):
+    pts = o.gen_points(seed, n)
+    if dup:
+        pts = o.duplicate_points(seed, n, pts)
+    sc = o.gen_scalars(seed + 1000, n, kind)
+    nbytes = (nbits + 7) // 8
+    packed = b"".join(sc[32 * i:32 * i + nbytes] for i in range(n)) if nbytes != 32 else sc
+    return pts, packed
+
+
+def main():
+    large = "--large" in sys.argv
+    build(ref=True)
+    o, r = Oracle(), Reference()
+    g = {"msm": [], "fft": [], "domain": []}
+    cases = [
+        # (seed, n, kind, nbits, dup)
+        (11, 1, 0, 255, False), (12, 2, 0, 255, False), (13, 3, 0, 255, False),
+        (14, 17, 0, 255, False), (15, 100, 0, 255, False), (16, 100, 0, 256, False),
+        (17, 100, 0, 64, False), (18, 100, 0, 1, False), (19, 100, 0, 7, False),
+        (20, 100, 0, 17, False), (21, 100, 0, 128, False), (22, 257, 1, 64, False),
+        (23, 1000, 2, 255, True), (24, 999, 0, 200, False),
+        (1, 4096, 0, 255, False),                      # plain MSM, n = 4096, seed 1
+        (2, 1 << 16, 0, 255, False), (3, 1 << 16, 1, 64, False), (4, 1 << 16, 2, 255, True),
+        (5, 1 << 16, 1, 255, False),
+    ]
+    if large:
+        cases += [(6, 1 << 20, 0, 255, False), (7, 1 << 22, 0, 255, False)]
+    for seed, n, kind, nbits, dup in cases:
+        t = time.time()
+        pts, sc = msm_inputs(o, seed, n, kind, nbits, dup)
+        res = r.msm(pts, sc, n, nbits)
+        g["msm"].append({"seed": seed, "n": n, "kind": kind, "nbits": nbits, "dup": dup,
+                         "compressed": res.hex()})
+        print("msm", seed, n, kind, nbits, dup, res.hex()[:16], "%.1fs" % (time.time() - t), flush=True)
+
+    for k in range(0, 17):
+        n = 1 << k
+        g["domain"].append({"n": n, "sha256": hashlib.sha256(r.domain(n)).hexdigest()})
+
+    fft_cases = [(31, 1), (32, 2), (33, 4), (34, 8), (35, 16), (36, 64), (37, 256), (38, 1024)]
+    if large:
+        fft_cases += [(39, 4096)]
+    for seed, n in fft_cases:
+        aff = o.gen_points(seed, n)
+        jac = o.jacobian_randomize(seed, n, aff)
+        d = r.domain(n)
+        for mode in ("fwd", "inv", "dfwd", "dinv", "dunscaled"):
+            t = time.time()
+            if mode == "fwd":
+                ok, out = r.p1_fft(jac, n, False)
+            elif mode == "inv":
+                ok, out = r.p1_fft(jac, n, True)
+            elif mode == "dfwd":
+                ok, out = r.p1_fft_with_domain(jac, n, d, n + 2, False)
+            elif mode == "dinv":
+                ok, out = r.p1_fft_with_domain(jac, n, d, n + 2, True)
+            else:
+                ok, out = r.p1_ifft_unscaled_with_domain(jac, n, d, n + 2)
+            assert ok
+            ser = b"".join(r.serialize(out[144 * i:144 * i + 144]) for i in range(n))
+            entry = {"seed": seed, "n": n, "mode": mode, "sha256": hashlib.sha256(ser).hexdigest()}
+            if n <= 16:
+                entry["serialized"] = ser.hex()
+            g["fft"].append(entry)
+            print("fft", seed, n, mode, "%.1fs" % (time.time() - t), flush=True)
+    if not large and os.path.exists(OUT):
+        # keep previously generated large cases
+        old = json.load(open(OUT))
+        have = {(c["seed"], c["n"]) for c in g["msm"]}
+        g["msm"] += [c for c in old["msm"] if (c["seed"], c["n"]) not in have]
+        havef = {(c["seed"], c["n"], c["mode"]) for c in g["fft"]}
+        g["fft"] += [c for c in old["fft"] if (c["seed"], c["n"], c["mode"]) not in havef]
+    json.dump(g, open(OUT, "w"), indent=1)
+    print("wrote", OUT)
+
+
+if __name__ == "__main__":
+    main()

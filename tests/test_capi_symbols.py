@@ -1,0 +1,50 @@
+"""CPU check: the C-ABI library builds for sm_103a, loads, and exports every
+function declared in include/*.h (no GPU call is made)."""
+import ctypes as C
+import glob
+import os
+import re
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared_functions():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        src = open(h).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        for m in re.finditer(r"^[A-Za-z_][\w \*]*?\b([a-z_][a-z0-9_]*)\s*\(", src, flags=re.M):
+            name = m.group(1)
+            if name not in ("defined", "if", "sizeof"):
+                names.add(name)
+    return names
+
+
+def test_header_declares_drop_in_entry_points():
+    names = _declared_functions()
+    for must in ("blst_p1s_mult_pippenger", "blst_p1s_mult_pippenger_scratch_sizeof",
+                 "blst_p1_fft", "blst_p1_fft_with_domain", "blst_p1_ifft_unscaled_with_domain",
+                 "blst_fr_fft_domain_len", "blst_fr_fft_domain_init"):
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol(gpu_binding):
+    gpu_binding.load()                       # builds with nvcc if needed; raises on failure
+    lib = C.CDLL(gpu_binding.LIB_PATH)
+    missing = [n for n in sorted(_declared_functions()) if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_scratch_sizeof_matches_reference_contract(gpu_binding, oracle):
+    # pure host functions: no device call
+    for n in (0, 1, 2, 5, 17, 256, 4096, 1 << 16, 1 << 20, 1 << 22):
+        assert gpu_binding.scratch_sizeof(n) == oracle.scratch_sizeof(n), n
+    assert gpu_binding.scratch_sizeof(4096) == 98304
+    assert gpu_binding.scratch_sizeof(1 << 16) == 786432
+    for w in (0, 1, 5, 24, 25):
+        exp = 0 if w < 1 or w > 24 else 192 << (w - 1)
+        assert gpu_binding.window_scratch_sizeof(w) == exp
+    for n in (0, 3, 6, 1 << 31):
+        assert gpu_binding.fr_fft_domain_len(n) == 0
+    for k in (0, 1, 10, 30):
+        assert gpu_binding.fr_fft_domain_len(1 << k) == (1 << k) + 2

@@ -1,0 +1,149 @@
+"""CPU checks: the oracle restatement against the reference's golden vectors,
+the seeded generators against each other, and (where the reference tree was
+present at build time) the oracle against the reference library itself."""
+import ctypes as C
+import hashlib
+import os
+
+import pytest
+
+import oracle as om
+
+
+def _msm_inputs(o, c):
+    n, nbits = c["n"], c["nbits"]
+    pts = o.gen_points(c["seed"], n)
+    if c["dup"]:
+        pts = o.duplicate_points(c["seed"], n, pts)
+    sc = o.gen_scalars(c["seed"] + 1000, n, c["kind"])
+    nb = (nbits + 7) // 8
+    if nb != 32:
+        sc = b"".join(sc[32 * i:32 * i + nb] for i in range(n))
+    return pts, sc
+
+
+def test_oracle_msm_matches_golden(golden, oracle):
+    cases = [c for c in golden["msm"] if c["n"] <= (1 << 16)]
+    assert len(cases) >= 18
+    for c in cases:
+        pts, sc = _msm_inputs(oracle, c)
+        got = oracle.msm(pts, sc, c["n"], c["nbits"])
+        assert got.hex() == c["compressed"], c
+
+
+def test_oracle_fft_matches_golden(golden, oracle):
+    for c in golden["fft"]:
+        n = c["n"]
+        if n > 256:
+            continue
+        aff = oracle.gen_points(c["seed"], n)
+        jac = oracle.jacobian_randomize(c["seed"], n, aff)
+        d = oracle.domain(n)
+        mode = c["mode"]
+        if mode == "fwd":
+            ok, out = oracle.p1_fft(jac, n, False)
+        elif mode == "inv":
+            ok, out = oracle.p1_fft(jac, n, True)
+        elif mode == "dfwd":
+            ok, out = oracle.p1_fft_with_domain(jac, n, d, n + 2, False)
+        elif mode == "dinv":
+            ok, out = oracle.p1_fft_with_domain(jac, n, d, n + 2, True)
+        else:
+            ok, out = oracle.p1_ifft_unscaled_with_domain(jac, n, d, n + 2)
+        assert ok
+        ser = b"".join(oracle.serialize(out[144 * i:144 * i + 144]) for i in range(n))
+        assert hashlib.sha256(ser).hexdigest() == c["sha256"], (n, mode)
+
+
+def test_oracle_domains_match_golden(golden, oracle):
+    for c in golden["domain"]:
+        assert hashlib.sha256(oracle.domain(c["n"])).hexdigest() == c["sha256"], c["n"]
+
+
+def test_oracle_naive_and_windows_agree(oracle):
+    n = 40
+    pts = oracle.gen_points(101, n)
+    sc = oracle.gen_scalars(102, n, 0)
+    ref = oracle.msm_naive(pts, sc, n, 255)
+    assert oracle.msm(pts, sc, n, 255) == ref
+    for w in (1, 2, 3, 5, 8, 13):
+        assert oracle.msm_window(pts, sc, n, 255, w) == ref
+
+
+def test_oracle_fft_round_trip_and_exponent(oracle):
+    """FFT-in-the-exponent: fft(i*G) == fr_fft(i)*G (reference test
+    BindingHeader_tests.cpp:480-569), and inverse(forward(x)) == x."""
+    n = 8
+    G = oracle.generator()
+    vals = b""
+    frs = b""
+    for i in range(n):
+        k = (i + 3).to_bytes(32, "little")
+        vals += oracle.mult(G, k, 256)
+        frs += oracle.fr_to_mont(k)
+    ok, fx = oracle.p1_fft(vals, n, False)
+    assert ok
+    ok, ff = oracle.fr_fft(frs, n, False)
+    assert ok
+    for i in range(n):
+        k = oracle.fr_from_mont(ff[32 * i:32 * i + 32])
+        assert oracle.compress(fx[144 * i:144 * i + 144]) == oracle.compress(oracle.mult(G, k, 256))
+    ok, back = oracle.p1_fft(fx, n, True)
+    assert ok
+    for i in range(n):
+        assert oracle.compress(back[144 * i:144 * i + 144]) == oracle.compress(vals[144 * i:144 * i + 144])
+
+
+def test_oracle_rejects_bad_fft_inputs(oracle):
+    jac = oracle.jacobian_randomize(5, 4, oracle.gen_points(5, 4))
+    d = oracle.domain(4)
+    ok, out = oracle.p1_fft(jac[:3 * 144], 3, False)
+    assert not ok
+    bad = bytearray(d)
+    bad[-1] ^= 1
+    ok, out = oracle.p1_fft_with_domain(jac, 4, bytes(bad), 6, False)
+    assert not ok and out == jac
+    ok, out = oracle.p1_fft_with_domain(jac, 4, d, 5, False)
+    assert not ok and out == jac
+
+
+def test_synth_matches_oracle_generator(oracle, synth):
+    for kind in (0, 1, 2):
+        for seed in (1, 7, 123456789):
+            assert synth.scalars(seed, 777, kind) == oracle.gen_scalars(seed, 777, kind), (seed, kind)
+    n = 500
+    pts = oracle.gen_points(9, n)
+    assert synth.point_scalars(9, n) == oracle.gen_scalars(9 ^ 0xA5A5A5A5, n, 0)
+    dup = oracle.duplicate_points(9, n, pts)
+    assert bytes(synth.apply_duplicates(bytearray(pts), 9, n)) == dup
+
+
+@pytest.mark.skipif(not om.reference_available(), reason="reference library not built here")
+def test_oracle_matches_reference_descriptor_arrays(oracle):
+    """Non-contiguous descriptor arrays and the fail-closed cases, oracle vs
+    the reference's own C ABI (reference tests C_api_tests.cpp:1517-1611)."""
+    ref = om.Reference()
+    n = 9
+    pts = bytearray(oracle.gen_points(55, n))
+    sc = bytearray(oracle.gen_scalars(56, n, 0))
+    pb = (C.c_char * len(pts)).from_buffer(pts)
+    sb = (C.c_char * len(sc)).from_buffer(sc)
+    base_p, base_s = C.addressof(pb), C.addressof(sb)
+    order = [3, 0, 5, 1, 8, 2, 7, 4, 6]
+    pa = (C.c_void_p * n)(*[base_p + 96 * i for i in order])
+    sa = (C.c_void_p * n)(*[base_s + 32 * i for i in order])
+    scratch = (C.c_uint64 * 4096)()
+    r1, r2 = bytearray(144), bytearray(144)
+    oracle.L.oracle_p1s_mult_pippenger((C.c_char * 144).from_buffer(r1), pa, n, sa, 255, scratch)
+    ref.L.blst_p1s_mult_pippenger((C.c_char * 144).from_buffer(r2), pa, n, sa, 255, scratch)
+    assert oracle.compress(bytes(r1)) == ref.compress(bytes(r2))
+    # mixed: two explicit heads then NULL continuation
+    pa2 = (C.c_void_p * 3)(base_p, base_p + 96, None)
+    sa2 = (C.c_void_p * 3)(base_s, base_s + 32, None)
+    oracle.L.oracle_p1s_mult_pippenger((C.c_char * 144).from_buffer(r1), pa2, n, sa2, 255, scratch)
+    ref.L.blst_p1s_mult_pippenger((C.c_char * 144).from_buffer(r2), pa2, n, sa2, 255, scratch)
+    assert oracle.compress(bytes(r1)) == ref.compress(bytes(r2))
+    # null scratch with n > 1 -> infinity in both
+    oracle.L.oracle_p1s_mult_pippenger((C.c_char * 144).from_buffer(r1), pa, n, sa, 255, None)
+    ref.L.blst_p1s_mult_pippenger((C.c_char * 144).from_buffer(r2), pa, n, sa, 255, None)
+    assert oracle.compress(bytes(r1)) == ref.compress(bytes(r2)) == bytes([0xC0]) + bytes(47)
