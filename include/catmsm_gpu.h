@@ -120,6 +120,21 @@ int catmsm_p1_affines_from_scalars(blst_p1_affine *out, const blst_byte *k32, si
 /* Same with device buffers on the library stream. */
 int catmsm_p1_affines_from_scalars_device(void *d_out, const void *d_k32, size_t n);
 
+/* Measured integer multiply-add throughput of the current device in
+ * tera-IMAD/s (independent 32-bit mad.lo chains on every SM; best of five
+ * launches), or a negative value on failure. */
+double catmsm_imad_peak(void);
+
+/* Per-stage CUDA-event timing of this thread's MSM pipeline.  Stages:
+ * 0 memset, 1 digits, 2 scan, 3 scatter, 4 accumulate, 5 fixup,
+ * 6 reduce (segments + windows + result copy), 7 host fold.  read returns the
+ * stage count and fills min(max, count) accumulated milliseconds. */
+void catmsm_profile(int enable);
+void catmsm_profile_reset(void);
+int catmsm_profile_read(double *ms, int max, long *calls);
+/* Total bucket entries (nonzero window digits) of the profiled MSM calls. */
+double catmsm_profile_entries(void);
+
 /* Field self-check: out[i] = a[i] * b[i] * R^-1 mod p (canonical), host
  * buffers of n blst_fp.  Returns 0 on success. */
 int catmsm_fp_mul(blst_fp *out, const blst_fp *a, const blst_fp *b, size_t n);

@@ -177,6 +177,34 @@ void oracle_p1s_mult_pippenger(op1 *ret, const op1a *const points[], size_t npoi
     mult_pippenger_common(ret, points, npoints, scalars, nbits, scratch, 0, 0);
 }
 
+/* blst_p1s_tile_pippenger (c_api.cpp:1585-1612 -> :883-936): one window's
+ * bucket fill + running-sum reduction starting at bit bit0.  Used as the
+ * bounded CPU-baseline sample: a full MSM is D such tiles plus a short fold. */
+void oracle_p1s_tile_pippenger(op1 *ret, const op1a *const points[], size_t npoints,
+                               const uint8_t *const scalars[], size_t nbits,
+                               uint64_t *scratch, size_t bit0, size_t window)
+{
+    memset(ret, 0, sizeof(*ret));
+    if (npoints == 0 || !valid_heads(points, scalars, npoints) || scratch == NULL ||
+        window < 1 || window > MAX_WINDOW || nbits == 0 || nbits > 256 || bit0 >= nbits)
+        return;
+    wextract we;
+    wextract_init(&we, bit0, window, nbits);
+    op1xyzz *buckets = (op1xyzz *)scratch;
+    memset(buckets, 0, sizeof(op1xyzz) << (we.encode_size - 1));
+    size_t nbytes = (nbits + 7) / 8;
+    const uint8_t *scalar = *scalars++;
+    const op1a *point = *points++;
+    for (size_t i = 0; i < npoints; i++) {
+        if (i) {
+            scalar = *scalars ? *scalars++ : scalar + nbytes;
+            point = *points ? *points++ : point + 1;
+        }
+        point_bucket(buckets, wextract_digit(&we, scalar), we.encode_size, point);
+    }
+    integrate_buckets(ret, buckets, we.encode_size - 1);
+}
+
 void oracle_p1s_mult_naive(op1 *ret, const op1a *points, size_t npoints,
                            const uint8_t *scalars, size_t nbits)
 {

@@ -86,6 +86,9 @@ void oracle_p1s_mult_pippenger(op1 *ret, const op1a *const points[], size_t npoi
 void oracle_p1s_mult_pippenger_window(op1 *ret, const op1a *const points[], size_t npoints,
                                       const uint8_t *const scalars[], size_t nbits,
                                       uint64_t *scratch, size_t window);
+void oracle_p1s_tile_pippenger(op1 *ret, const op1a *const points[], size_t npoints,
+                               const uint8_t *const scalars[], size_t nbits,
+                               uint64_t *scratch, size_t bit0, size_t window);
 /* Naive sum of k_i * P_i (the reference tests' algorithmic oracle). */
 void oracle_p1s_mult_naive(op1 *ret, const op1a *points, size_t npoints,
                            const uint8_t *scalars, size_t nbits);

@@ -74,6 +74,7 @@ class Oracle(_Common):
         L.oracle_p1s_mult_pippenger.argtypes = [_vp, _vp, _sz, _vp, _sz, _vp]
         L.oracle_p1s_mult_pippenger_window.argtypes = [_vp, _vp, _sz, _vp, _sz, _vp, _sz]
         L.oracle_p1s_mult_naive.argtypes = [_vp, _vp, _sz, _vp, _sz]
+        L.oracle_p1s_tile_pippenger.argtypes = [_vp, _vp, _sz, _vp, _sz, _vp, _sz, _sz]
         L.oracle_pippenger_window_size.restype = _sz
         L.oracle_pippenger_window_size.argtypes = [_sz]
         L.op1_compress.argtypes = [_vp, _vp]
@@ -184,6 +185,19 @@ class Oracle(_Common):
         ret = bytearray(P1)
         self.L.oracle_p1s_mult_pippenger_window(_buf(ret), parr, n, sarr, nbits, scratch, window)
         return self.compress(bytes(ret))
+
+    def tile_seconds(self, points, scalars, n, nbits, bit0, window, reps=1) -> float:
+        """Wall time of `reps` single-window tiles (bounded CPU sample)."""
+        import time
+        pbuf, sbuf = _buf(bytearray(points)), _buf(bytearray(scalars))
+        parr = (C.c_void_p * 2)(C.cast(pbuf, C.c_void_p), None)
+        sarr = (C.c_void_p * 2)(C.cast(sbuf, C.c_void_p), None)
+        scratch = (C.c_uint64 * ((192 << max(0, window - 1)) // 8 + 1))()
+        ret = bytearray(P1)
+        t = time.perf_counter()
+        for _ in range(reps):
+            self.L.oracle_p1s_tile_pippenger(_buf(ret), parr, n, sarr, nbits, scratch, bit0, window)
+        return time.perf_counter() - t
 
     def msm_naive(self, points, scalars, n, nbits) -> bytes:
         ret = bytearray(P1)

@@ -74,6 +74,16 @@ def load(build_if_missing=True):
     L.catmsm_p1_affines_from_scalars_device.argtypes = [_vp, _vp, _sz]
     L.catmsm_fp_mul.restype = C.c_int
     L.catmsm_fp_mul.argtypes = [_vp, _vp, _vp, _sz]
+    L.catmsm_imad_peak.restype = C.c_double
+    L.catmsm_imad_peak.argtypes = []
+    L.catmsm_profile.restype = None
+    L.catmsm_profile.argtypes = [C.c_int]
+    L.catmsm_profile_reset.restype = None
+    L.catmsm_profile_reset.argtypes = []
+    L.catmsm_profile_entries.restype = C.c_double
+    L.catmsm_profile_entries.argtypes = []
+    L.catmsm_profile_read.restype = C.c_int
+    L.catmsm_profile_read.argtypes = [_vp, C.c_int, _vp]
     _lib = L
     return L
 
@@ -196,3 +206,31 @@ def launch_count() -> int:
 
 def msm_window(n: int) -> int:
     return load().catmsm_msm_window(n)
+
+
+STAGES = ("memset", "digits", "scan", "scatter", "accumulate", "fixup", "reduce", "host_fold")
+
+
+def imad_peak_tera() -> float:
+    """Measured device IMAD throughput, tera-IMAD/s."""
+    return load().catmsm_imad_peak()
+
+
+def profile(enable: bool) -> None:
+    load().catmsm_profile(1 if enable else 0)
+
+
+def profile_reset() -> None:
+    load().catmsm_profile_reset()
+
+
+def profile_read():
+    """{stage: accumulated ms}, number of profiled calls."""
+    ms = (C.c_double * len(STAGES))()
+    calls = C.c_long(0)
+    load().catmsm_profile_read(ms, len(STAGES), C.byref(calls))
+    return dict(zip(STAGES, list(ms))), calls.value
+
+
+def profile_entries() -> float:
+    return load().catmsm_profile_entries()

@@ -70,13 +70,23 @@ struct FftWork {
     DevBuf values, roots, glv, scratch;
 };
 
+// Per-stage CUDA-event timing of the MSM pipeline (off by default).
+constexpr int kMsmStages = 8;   // memset, digits, scan, scatter, accumulate, fixup, reduce, host fold
+struct StageProfile {
+    bool enabled = false;
+    cudaEvent_t ev[kMsmStages + 1] = {};
+    double ms[kMsmStages] = {};
+    long calls = 0;
+    double entries = 0;   // bucket entries (nonzero digits) accumulated
+};
+
 struct Ctx {
     int device = -1;
     cudaStream_t stream = nullptr;
     MsmWork msm;
     FftWork fft;
     PinnedBuf h_points, h_scalars, h_out, h_values;
-    cudaEvent_t ev_a = nullptr, ev_b = nullptr;
+    StageProfile prof;
 };
 
 // Per-thread context bound to the thread's current device.

@@ -400,22 +400,37 @@ cudaError_t msm_device(Ctx* ctx, const void* d_points, const uint8_t* d_scalars,
         return cudaErrorMemoryAllocation;
     uint32_t* total = offsets + M;
 
+    StageProfile& P = ctx->prof;
+    if (P.enabled && !P.ev[0]) {
+        for (int i = 0; i <= kMsmStages; i++) CATMSM_CHECK(cudaEventCreate(&P.ev[i]));
+    }
+    auto mark = [&](int i) {
+        if (P.enabled) cudaEventRecord(P.ev[i], st);
+    };
+    mark(0);
     CATMSM_CHECK(cudaMemsetAsync(counts, 0, M * 4, st));
     CATMSM_CHECK(cudaMemsetAsync(buckets, 0, M * sizeof(xyzz), st));
+    mark(1);
     k_digits<<<div_up(n, 256), 256, 0, st>>>(d_scalars, stride, (uint32_t)n, nbits, c, D, digits, ranks, counts);
+    mark(2);
     k_scan_local<<<nblocks, kScanThreads, 0, st>>>(counts, offsets, bsums, (uint32_t)M);
     k_scan_top<<<1, kScanThreads, 0, st>>>(bsums, nblocks, total);
     k_scan_add<<<div_up(M, 256), 256, 0, st>>>(offsets, bsums, (uint32_t)M);
+    mark(3);
     k_scatter<<<div_up(nD, 256), 256, 0, st>>>(digits, ranks, offsets, (uint32_t)n, (uint32_t)nD, sorted_pt,
                                               sorted_key);
+    mark(4);
     k_accumulate<<<div_up(chunks, 128), 128, 0, st>>>((const affine*)d_points, sorted_pt, sorted_key, total, L,
                                                       buckets, head, tail);
+    mark(5);
     k_fixup<<<div_up(chunks, 128), 128, 0, st>>>(sorted_key, total, L, buckets, head, tail);
+    mark(6);
     k_reduce_seg<<<div_up((size_t)D * T, 128), 128, 0, st>>>(buckets, B, S, D, seg);
     k_reduce_win<<<D, kWinThreads, 0, st>>>(seg, T, wins);
     g_stats.launches += 9;
     CATMSM_CHECK(cudaGetLastError());
     CATMSM_CHECK(cudaMemcpyAsync(h_wins, wins, (size_t)D * sizeof(xyzz), cudaMemcpyDeviceToHost, st));
+    mark(7);
     CATMSM_CHECK(cudaStreamSynchronize(st));
 
     using namespace catmsm_host;
@@ -431,6 +446,19 @@ cudaError_t msm_device(Ctx* ctx, const void* d_points, const uint8_t* d_scalars,
     hjac norm;
     normalize(norm, ret);
     std::memcpy(out, &norm, 144);
+    if (P.enabled) {
+        CATMSM_CHECK(cudaEventRecord(P.ev[kMsmStages], st));
+        CATMSM_CHECK(cudaEventSynchronize(P.ev[kMsmStages]));
+        for (int i = 0; i < kMsmStages; i++) {
+            float ms = 0.f;
+            CATMSM_CHECK(cudaEventElapsedTime(&ms, P.ev[i], P.ev[i + 1]));
+            P.ms[i] += ms;
+        }
+        uint32_t E = 0;
+        CATMSM_CHECK(cudaMemcpy(&E, total, 4, cudaMemcpyDeviceToHost));
+        P.entries += E;
+        P.calls++;
+    }
     return cudaSuccess;
 }
 
