@@ -121,9 +121,12 @@ int catmsm_p1_affines_from_scalars(blst_p1_affine *out, const blst_byte *k32, si
 int catmsm_p1_affines_from_scalars_device(void *d_out, const void *d_k32, size_t n);
 
 /* Measured integer multiply-add throughput of the current device in
- * tera-IMAD/s (independent 32-bit mad.lo chains on every SM; best of five
- * launches), or a negative value on failure. */
+ * tera-IMAD/s: independent 32-bit chains on every SM, the better of the
+ * mad.lo.u32 form and the mad.wide.u32 form (one instruction yielding both
+ * product halves, counted as two); negative on failure.  _form measures one
+ * form only (wide = 0: mad.lo, 1: mad.wide). */
 double catmsm_imad_peak(void);
+double catmsm_imad_peak_form(int wide);
 
 /* Per-stage CUDA-event timing of this thread's MSM pipeline.  Stages:
  * 0 memset, 1 digits, 2 scan, 3 scatter, 4 accumulate, 5 fixup,

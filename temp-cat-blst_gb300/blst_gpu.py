@@ -76,6 +76,8 @@ def load(build_if_missing=True):
     L.catmsm_fp_mul.argtypes = [_vp, _vp, _vp, _sz]
     L.catmsm_imad_peak.restype = C.c_double
     L.catmsm_imad_peak.argtypes = []
+    L.catmsm_imad_peak_form.restype = C.c_double
+    L.catmsm_imad_peak_form.argtypes = [C.c_int]
     L.catmsm_profile.restype = None
     L.catmsm_profile.argtypes = [C.c_int]
     L.catmsm_profile_reset.restype = None
@@ -214,6 +216,12 @@ STAGES = ("memset", "digits", "scan", "scatter", "accumulate", "fixup", "reduce"
 def imad_peak_tera() -> float:
     """Measured device IMAD throughput, tera-IMAD/s."""
     return load().catmsm_imad_peak()
+
+
+def imad_peak_forms():
+    """(mad.lo, mad.wide) measured tera-IMAD/s."""
+    L = load()
+    return L.catmsm_imad_peak_form(0), L.catmsm_imad_peak_form(1)
 
 
 def profile(enable: bool) -> None:

@@ -63,7 +63,7 @@ struct PinnedBuf {
 // Device workspaces of one MSM pipeline instance.
 struct MsmWork {
     DevBuf points, scalars, digits, ranks, counts, offsets, block_sums, sorted_pt, sorted_key,
-        buckets, head, tail, seg, wins, total, status;
+        buckets, head, tail, seg, wins, total, status, misc;
 };
 
 struct FftWork {

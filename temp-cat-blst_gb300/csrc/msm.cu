@@ -14,10 +14,12 @@
 //                    fixed chunk of L sorted entries and folds runs of equal
 //                    keys with XYZZ mixed adds; runs that cross a chunk edge
 //                    go to head/tail carry slots.
-//   5. k_fixup       joins carry slots of buckets that span chunks.
-//   6. k_reduce_seg  running-sum reduction sum_d d * S_d over segments of S
-//                    buckets, plus (segment offset) * (segment sum).
-//   7. k_reduce_win  block tree-sum of the segments of each window.
+//   5. k_fixup       joins carry slots of buckets that span chunks (block-wide
+//                    tree for buckets spanning many chunks: k_fixup_hot).
+//   6. k_reduce_level  sum_d d * S_d per window as a tree of running sums:
+//                    fan-in 8 over the buckets, then fan-in 2 levels whose
+//                    dependent chains are ~3 group operations (no scalar
+//                    multiplications); one launch per level.
 //   8. host          folds the D window sums: ret = 2^c ret + W_w, top first
 //                    (reference multi_scalar.cpp:913-922), then normalises.
 #include "common.cuh"
@@ -256,10 +258,21 @@ __global__ void __launch_bounds__(128) k_accumulate(const affine* __restrict__ p
 }
 
 // ----------------------------------------------------------------- 5. fixup
+// A bucket whose entries cross chunk edges has partial sums in tail[t0]
+// (its first chunk) and head[t0+1 .. t1].  Short spans are joined by one
+// thread; spans longer than kHotSpan chunks (a bucket holding a large share
+// of all entries, e.g. a carry-only top window or repeated scalars) go to a
+// list that k_fixup_hot reduces with a whole block per bucket, so no serial
+// chain grows with n.
+constexpr uint32_t kHotSpan = 16;
+constexpr int kHotThreads = 128;
+
 __global__ void __launch_bounds__(128) k_fixup(const uint32_t* __restrict__ sorted_key,
+                                               const uint32_t* __restrict__ offsets,
                                                const uint32_t* __restrict__ total_ptr, uint32_t L,
                                                xyzz* __restrict__ buckets, const xyzz* __restrict__ head,
-                                               const xyzz* __restrict__ tail)
+                                               const xyzz* __restrict__ tail, uint2* __restrict__ hot_list,
+                                               uint32_t* __restrict__ hot_count)
 {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t E = *total_ptr;
@@ -271,75 +284,98 @@ __global__ void __launch_bounds__(128) k_fixup(const uint32_t* __restrict__ sort
     const bool single = sorted_key[start] == last;
     const bool starts_before = start > 0 && sorted_key[start - 1] == sorted_key[start];
     if (single && starts_before) return;                               // a middle chunk
+    const uint32_t t1 = (offsets[last + 1] - 1) / L;                   // last chunk of this bucket
+    if (t1 - t + 1 > kHotSpan) {
+        const uint32_t h = atomicAdd(hot_count, 1u);
+        hot_list[h] = make_uint2(last, t);
+        return;
+    }
     xyzz acc, part;
     load_xyzz(acc, tail + t);
-    for (uint32_t u = t + 1;; u++) {
+    for (uint32_t u = t + 1; u <= t1; u++) {
         load_xyzz(part, head + u);
         xyzz_add(acc, part);
-        const size_t s = (size_t)u * L;
-        const uint32_t e = (uint32_t)min((size_t)E, s + L);
-        const bool u_single = sorted_key[e - 1] == last;
-        const bool u_cont = e < E && sorted_key[e] == last;
-        if (!(u_single && u_cont)) break;
     }
     store_xyzz(buckets + last, acc);
 }
 
-// ----------------------------------------------------------------- 6/7. reduce
-__global__ void __launch_bounds__(128) k_reduce_seg(const xyzz* __restrict__ buckets, uint32_t B,
-                                                    uint32_t S, uint32_t D, xyzz* __restrict__ seg_out)
+__global__ void __launch_bounds__(kHotThreads) k_fixup_hot(const uint2* __restrict__ hot_list,
+                                                           const uint32_t* __restrict__ hot_count,
+                                                           const uint32_t* __restrict__ offsets, uint32_t L,
+                                                           xyzz* __restrict__ buckets, const xyzz* __restrict__ head,
+                                                           const xyzz* __restrict__ tail)
 {
-    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t T = B / S;
-    if (t >= D * T) return;
-    const uint32_t w = t / T, s = t % T;
-    const xyzz* base = buckets + (size_t)w * B + (size_t)s * S;
-    xyzz acc, tri, b;
-    xyzz_set_inf(acc);
-    xyzz_set_inf(tri);
-    for (int j = (int)S - 1; j >= 0; j--) {
-        load_xyzz(b, base + j);
-        xyzz_add(acc, b);
-        xyzz_add(tri, acc);
-    }
-    // tri += (s*S) * acc : the digits of this segment start at s*S + 1
-    const uint32_t k = s * S;
-    if (k) {
-        xyzz m;
-        xyzz_set_inf(m);
-        for (int bit = 31 - __clz(k); bit >= 0; bit--) {
-            xyzz_dbl(m);
-            if ((k >> bit) & 1) xyzz_add(m, acc);
+    __shared__ xyzz sh[kHotThreads];
+    const uint32_t nh = *hot_count;
+    for (uint32_t h = blockIdx.x; h < nh; h += gridDim.x) {
+        const uint2 e = hot_list[h];
+        const uint32_t key = e.x, t0 = e.y;
+        const uint32_t span = (offsets[key + 1] - 1) / L - t0 + 1;
+        xyzz acc, part;
+        xyzz_set_inf(acc);
+        for (uint32_t i = threadIdx.x; i < span; i += kHotThreads) {
+            load_xyzz(part, i == 0 ? tail + t0 : head + t0 + i);
+            xyzz_add(acc, part);
         }
-        xyzz_add(tri, m);
-    }
-    store_xyzz(seg_out + t, tri);
-}
-
-constexpr int kWinThreads = 128;
-
-__global__ void __launch_bounds__(kWinThreads) k_reduce_win(const xyzz* __restrict__ seg, uint32_t T,
-                                                            xyzz* __restrict__ wins)
-{
-    __shared__ xyzz sh[kWinThreads];
-    const uint32_t w = blockIdx.x;
-    xyzz acc, b;
-    xyzz_set_inf(acc);
-    for (uint32_t s = threadIdx.x; s < T; s += kWinThreads) {
-        load_xyzz(b, seg + (size_t)w * T + s);
-        xyzz_add(acc, b);
-    }
-    sh[threadIdx.x] = acc;
-    __syncthreads();
-    for (int h = kWinThreads / 2; h > 0; h >>= 1) {
-        if ((int)threadIdx.x < h) {
-            xyzz a = sh[threadIdx.x];
-            xyzz_add(a, sh[threadIdx.x + h]);
-            sh[threadIdx.x] = a;
+        sh[threadIdx.x] = acc;
+        __syncthreads();
+        for (int k = kHotThreads / 2; k > 0; k >>= 1) {
+            if ((int)threadIdx.x < k) {
+                xyzz a = sh[threadIdx.x];
+                xyzz_add(a, sh[threadIdx.x + k]);
+                sh[threadIdx.x] = a;
+            }
+            __syncthreads();
         }
+        if (threadIdx.x == 0) store_xyzz(buckets + key, sh[0]);
         __syncthreads();
     }
-    if (threadIdx.x == 0) store_xyzz(wins + w, sh[0]);
+}
+
+// ----------------------------------------------------------------- 6/7. reduce
+// Window sum W = sum_{b<B} (b+1) S_b.  Write F0(x) = sum_i i x_i.  Grouping the
+// inputs of a level in runs of F (node u owns children uF .. uF+F-1):
+//   F0(x) = sum_u T_u + F0(F r),  r_u = sum_j x_{uF+j},  T_u = sum_j j x_{uF+j}
+// so every node emits Q_u = T_u + (its children's Q) and A_u = F r_u, and the
+// root's Q is the window sum.  Level 1 uses weights j+1 (giving W directly)
+// with fan-in 8: a 2-addition-per-bucket running sum that keeps every SM
+// busy.  Upper levels use fan-in 2 (one addition, one doubling, two Q
+// additions), keeping the dependent chain per level short: with few threads
+// the cost of a level is its serial latency, not its work.
+__global__ void __launch_bounds__(128) k_reduce_level(const xyzz* __restrict__ inA, const xyzz* __restrict__ inQ,
+                                                      uint32_t m_in, uint32_t F, uint32_t lgF, uint32_t D,
+                                                      int first, xyzz* __restrict__ outA, xyzz* __restrict__ outQ)
+{
+    const uint32_t m_out = (m_in + F - 1) / F;
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= D * m_out) return;
+    const uint32_t w = t / m_out, u = t % m_out;
+    const uint32_t c0 = u * F;
+    const uint32_t cnt = min(F, m_in - c0);
+    const xyzz* a = inA + (size_t)w * m_in + c0;
+    xyzz r, tt, b;
+    xyzz_set_inf(r);
+    xyzz_set_inf(tt);
+    for (int j = (int)cnt - 1; j >= 1; j--) {
+        load_xyzz(b, a + j);
+        xyzz_add(r, b);
+        xyzz_add(tt, r);
+    }
+    load_xyzz(b, a);
+    xyzz_add(r, b);
+    if (first) xyzz_add(tt, r);
+    if (inQ) {
+        const xyzz* q = inQ + (size_t)w * m_in + c0;
+        for (uint32_t j = 0; j < cnt; j++) {
+            load_xyzz(b, q + j);
+            xyzz_add(tt, b);
+        }
+    }
+    if (m_out > 1) {
+        for (uint32_t k = 0; k < lgF; k++) xyzz_dbl(r);
+        store_xyzz(outA + (size_t)w * m_out + u, r);
+    }
+    store_xyzz(outQ + (size_t)w * m_out + u, tt);
 }
 
 // ----------------------------------------------------------------- host driver
@@ -377,9 +413,9 @@ cudaError_t msm_device(Ctx* ctx, const void* d_points, const uint8_t* d_scalars,
     if (L < 4) L = 4;
     if (L > 64) L = 64;
     const size_t chunks = (nD + L - 1) / L;
-    uint32_t S = 8;
-    if (S > B) S = B;
-    const uint32_t T = B / S;
+    const uint32_t S = 8;                         // reduction fan-in per level
+    const size_t lvl1 = (size_t)D * ((B + S - 1) / S);
+    const size_t lvl2 = (size_t)D * ((B + 2 * S - 1) / (2 * S)) + D;
 
     uint32_t* digits = (uint32_t*)W.digits.get(nD * 4);
     uint32_t* ranks = (uint32_t*)W.ranks.get(nD * 4);
@@ -392,11 +428,13 @@ cudaError_t msm_device(Ctx* ctx, const void* d_points, const uint8_t* d_scalars,
     xyzz* buckets = (xyzz*)W.buckets.get(M * sizeof(xyzz));
     xyzz* head = (xyzz*)W.head.get(chunks * sizeof(xyzz));
     xyzz* tail = (xyzz*)W.tail.get(chunks * sizeof(xyzz));
-    xyzz* seg = (xyzz*)W.seg.get((size_t)D * T * sizeof(xyzz));
+    xyzz* seg = (xyzz*)W.seg.get(2 * (lvl1 + lvl2) * sizeof(xyzz));
     xyzz* wins = (xyzz*)W.wins.get((size_t)D * sizeof(xyzz));
     uint64_t* h_wins = (uint64_t*)ctx->h_out.get((size_t)D * sizeof(xyzz));
+    uint32_t* hot_count = (uint32_t*)W.status.get(256 + chunks * sizeof(uint2));
+    uint2* hot_list = reinterpret_cast<uint2*>(hot_count + 64);
     if (!digits || !ranks || !counts || !offsets || !bsums || !sorted_pt || !sorted_key || !buckets ||
-        !head || !tail || !seg || !wins || !h_wins)
+        !head || !tail || !seg || !wins || !h_wins || !hot_count)
         return cudaErrorMemoryAllocation;
     uint32_t* total = offsets + M;
 
@@ -410,6 +448,7 @@ cudaError_t msm_device(Ctx* ctx, const void* d_points, const uint8_t* d_scalars,
     mark(0);
     CATMSM_CHECK(cudaMemsetAsync(counts, 0, M * 4, st));
     CATMSM_CHECK(cudaMemsetAsync(buckets, 0, M * sizeof(xyzz), st));
+    CATMSM_CHECK(cudaMemsetAsync(hot_count, 0, 4, st));
     mark(1);
     k_digits<<<div_up(n, 256), 256, 0, st>>>(d_scalars, stride, (uint32_t)n, nbits, c, D, digits, ranks, counts);
     mark(2);
@@ -423,11 +462,33 @@ cudaError_t msm_device(Ctx* ctx, const void* d_points, const uint8_t* d_scalars,
     k_accumulate<<<div_up(chunks, 128), 128, 0, st>>>((const affine*)d_points, sorted_pt, sorted_key, total, L,
                                                       buckets, head, tail);
     mark(5);
-    k_fixup<<<div_up(chunks, 128), 128, 0, st>>>(sorted_key, total, L, buckets, head, tail);
+    k_fixup<<<div_up(chunks, 128), 128, 0, st>>>(sorted_key, offsets, total, L, buckets, head, tail, hot_list,
+                                                 hot_count);
+    k_fixup_hot<<<2 * kSMs, kHotThreads, 0, st>>>(hot_list, hot_count, offsets, L, buckets, head, tail);
     mark(6);
-    k_reduce_seg<<<div_up((size_t)D * T, 128), 128, 0, st>>>(buckets, B, S, D, seg);
-    k_reduce_win<<<D, kWinThreads, 0, st>>>(seg, T, wins);
-    g_stats.launches += 9;
+    {
+        // level 1: fan-in 8 over the buckets; then fan-in 2 to the root
+        xyzz* bufA[2] = {seg, seg + 2 * lvl1};
+        xyzz* bufQ[2] = {seg + lvl1, seg + 2 * lvl1 + lvl2};
+        const xyzz* inA = buckets;
+        const xyzz* inQ = nullptr;
+        uint32_t m = B, pp = 0;
+        bool first = true;
+        while (m > 1) {
+            const uint32_t F = first ? S : 2, lgF = first ? 3 : 1;
+            const uint32_t m_out = (m + F - 1) / F;
+            k_reduce_level<<<div_up((size_t)D * m_out, 128), 128, 0, st>>>(inA, inQ, m, F, lgF, D, first ? 1 : 0,
+                                                                          bufA[pp], bufQ[pp]);
+            g_stats.launches++;
+            inA = bufA[pp];
+            inQ = bufQ[pp];
+            pp ^= 1;
+            m = m_out;
+            first = false;
+        }
+        CATMSM_CHECK(cudaMemcpyAsync(wins, inQ ? inQ : inA, (size_t)D * sizeof(xyzz), cudaMemcpyDeviceToDevice, st));
+    }
+    g_stats.launches += 8;
     CATMSM_CHECK(cudaGetLastError());
     CATMSM_CHECK(cudaMemcpyAsync(h_wins, wins, (size_t)D * sizeof(xyzz), cudaMemcpyDeviceToHost, st));
     mark(7);

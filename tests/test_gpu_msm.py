@@ -116,13 +116,14 @@ def test_msm_fail_closed_edge_cases(gpu, oracle, synth):
     pts_inf[96 * 5:96 * 6] = bytes(96)
     assert oracle.compress(gpu.p1s_mult_pippenger(bytes(pts_inf), sc, n, 255)) == \
         oracle.msm(bytes(pts_inf), sc, n, 255)
-    # opposite points cancel, equal points double
+    # equal points double inside a bucket; k P + (r - k) P cancels to infinity
     P = pts[:96]
-    negP = oracle.affine_serialize(P)  # placeholder to keep oracle warm
     k = (5).to_bytes(32, "little")
     twice = gpu.p1s_mult_pippenger(P + P, k + k, 2, 255)
     assert oracle.compress(twice) == oracle.msm(P + P, k + k, 2, 255)
-    assert negP
+    kk = int.from_bytes(sc[:32], "little")
+    cancel = sc[:32] + (R - kk).to_bytes(32, "little")
+    assert oracle.compress(gpu.p1s_mult_pippenger(P + P, cancel, 2, 255)) == INF48
 
 
 def test_msm_descriptor_arrays(gpu, oracle, synth):
@@ -170,3 +171,28 @@ def test_msm_linearity_full_size(gpu, oracle, synth):
         acc %= R
     exp = oracle.compress(oracle.mult(oracle.generator(), acc.to_bytes(32, "little"), 256))
     assert got == exp
+
+
+def test_msm_hot_buckets(gpu, oracle, synth):
+    """Every window puts all points in one bucket (equal scalars): the
+    chunk-spanning fixup must stay parallel and exact."""
+    n = 1 << 16
+    pts = oracle.gen_points(31, n)
+    k = synth.scalars(32, 1, 0)
+    sc = k * n
+    assert oracle.compress(gpu.p1s_mult_pippenger(pts, sc, n, 255)) == oracle.msm(pts, sc, n, 255)
+
+
+@pytest.mark.parametrize("window", [2, 5, 8, 13, 15, 16, 17, 20])
+def test_msm_device_windows(gpu, oracle, synth, window):
+    """Device-resident entry point over every window width class, including
+    widths where 255 is a multiple of c (a carry-only top window)."""
+    import torch
+    n = 20000
+    pts = oracle.gen_points(40 + window, n)
+    sc = synth.scalars(41 + window, n, 0)
+    dp = torch.frombuffer(bytearray(pts), dtype=torch.uint8).cuda()
+    ds = torch.frombuffer(bytearray(sc), dtype=torch.uint8).cuda()
+    torch.cuda.synchronize()
+    got = gpu.msm_device(dp.data_ptr(), ds.data_ptr(), 32, n, 255, window)
+    assert oracle.compress(got) == oracle.msm(pts, sc, n, 255)
