@@ -8,7 +8,7 @@
 #include "catmsm_internal.h"
 #include "host_curve.hpp"
 #include "host_fr.hpp"
-#include "../../include/catmsm_gpu.h"
+#include "catmsm_gpu.h"
 
 #include <climits>
 #include <cstring>

@@ -9,7 +9,7 @@
 // against it (576 IMAD per 381-bit Montgomery multiplication).
 #include "common.cuh"
 #include "catmsm_internal.h"
-#include "../../include/catmsm_gpu.h"
+#include "catmsm_gpu.h"
 
 namespace catmsm {
 
