@@ -138,6 +138,29 @@ int catmsm_profile_read(double *ms, int max, long *calls);
 /* Total bucket entries (nonzero window digits) of the profiled MSM calls. */
 double catmsm_profile_entries(void);
 
+/* MSM that allocates nothing -- no counterpart in the reference library.
+ * For callers that must not allocate device memory at call time (for example
+ * when another framework has reserved nearly all GPU memory in its own pool,
+ * or on latency-critical paths where cudaMalloc/cudaFree could synchronise the
+ * device).  ret = sum_i k_i * P_i for CONTIGUOUS host arrays: npoints affine
+ * points and npoints scalars of ceil(nbits/8) little-endian bytes each.  All
+ * device work uses one fixed scratch array (7,167,488 bytes) that every GPU
+ * loading the library holds until the process exits; no cudaMalloc, cudaFree,
+ * pinned buffer, stream creation or heap allocation happens in the call.
+ * Limits: npoints <= CATMSM_NOALLOC_MAX_POINTS and nbits <= 256, else the call
+ * returns CATMSM_NOALLOC_TOO_LARGE and writes infinity.  Returns 0 on success
+ * (npoints == 0 or nbits == 0 give infinity), CATMSM_NOALLOC_BAD_ARGUMENT for
+ * NULL pointers, or a cudaError_t value.  Runs on the per-thread default
+ * stream and returns when the result is in *ret.  All calls share the one
+ * scratch array, so calls that overlap on the GPU race: serialise them.  The
+ * first call on a device looks up the array's address there; make it before
+ * any stream capture. */
+#define CATMSM_NOALLOC_MAX_POINTS 4096
+#define CATMSM_NOALLOC_BAD_ARGUMENT (-1)
+#define CATMSM_NOALLOC_TOO_LARGE (-2)
+int catmsm_p1s_mult_pippenger_noalloc(blst_p1 *ret, const blst_p1_affine *points, size_t npoints,
+                                      const blst_byte *scalars, size_t nbits);
+
 /* Field self-check: out[i] = a[i] * b[i] * R^-1 mod p (canonical), host
  * buffers of n blst_fp.  Returns 0 on success. */
 int catmsm_fp_mul(blst_fp *out, const blst_fp *a, const blst_fp *b, size_t n);
