@@ -161,6 +161,29 @@ double catmsm_profile_entries(void);
 int catmsm_p1s_mult_pippenger_noalloc(blst_p1 *ret, const blst_p1_affine *points, size_t npoints,
                                       const blst_byte *scalars, size_t nbits);
 
+/* ---- Batched commitments over a resident basis (no reference counterpart;
+ * the nearest reference API is the fixed-base wbits MSM, blst/c_api.cpp:1310-1369).
+ * catmsm_basis_create uploads n affine points (host) to the current device
+ * and builds fixed-base tables T[w][i] = 2^(c w) P_i (window c: 0 = 11); NULL
+ * on failure.  catmsm_basis_msm_batch computes nmsm MSMs in one pass:
+ * out[j] = sum_{i < counts[j]} k_{j,i} P_i, where the k_{j,i} are 32-byte
+ * little-endian 256-bit scalars, concatenated MSM by MSM; counts[j] <= n.
+ * Results are Jacobian blst_p1 (not normalised; z = 0 for infinity), as the
+ * reference MSM returns them.  use_graph != 0 replays the batch's device
+ * sequence as one CUDA graph launch (captured on first use per batch size).
+ * Calls on one basis must not overlap (one stream, one workspace per basis).
+ * catmsm_basis_autotune times (window, chunk) candidates on a caller batch,
+ * keeps the fastest, and remembers it per (GPU, n, nmsm, points-per-MSM
+ * class) in the text file $CATMSM_TUNE_CACHE (default ~/.cache/catmsm_tune.txt);
+ * force != 0 re-tunes.  All return 0 or a cudaError_t value. */
+void *catmsm_basis_create(const blst_p1_affine *points, size_t n, size_t window);
+void catmsm_basis_destroy(void *basis);
+int catmsm_basis_config(void *basis, size_t *window, size_t *chunk);
+int catmsm_basis_set_config(void *basis, size_t window, size_t chunk);
+int catmsm_basis_msm_batch(void *basis, blst_p1 *out, size_t nmsm, const size_t *counts,
+                           const blst_byte *scalars, int use_graph);
+int catmsm_basis_autotune(void *basis, size_t nmsm, const size_t *counts, const blst_byte *scalars, int force);
+
 /* Field self-check: out[i] = a[i] * b[i] * R^-1 mod p (canonical), host
  * buffers of n blst_fp.  Returns 0 on success. */
 int catmsm_fp_mul(blst_fp *out, const blst_fp *a, const blst_fp *b, size_t n);

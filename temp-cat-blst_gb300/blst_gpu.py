@@ -82,6 +82,18 @@ def load(build_if_missing=True):
     L.catmsm_profile.argtypes = [C.c_int]
     L.catmsm_profile_reset.restype = None
     L.catmsm_profile_reset.argtypes = []
+    L.catmsm_basis_create.restype = C.c_void_p
+    L.catmsm_basis_create.argtypes = [_vp, _sz, _sz]
+    L.catmsm_basis_destroy.restype = None
+    L.catmsm_basis_destroy.argtypes = [_vp]
+    L.catmsm_basis_config.restype = C.c_int
+    L.catmsm_basis_config.argtypes = [_vp, _vp, _vp]
+    L.catmsm_basis_set_config.restype = C.c_int
+    L.catmsm_basis_set_config.argtypes = [_vp, _sz, _sz]
+    L.catmsm_basis_msm_batch.restype = C.c_int
+    L.catmsm_basis_msm_batch.argtypes = [_vp, _vp, _sz, _vp, _vp, C.c_int]
+    L.catmsm_basis_autotune.restype = C.c_int
+    L.catmsm_basis_autotune.argtypes = [_vp, _sz, _vp, _vp, C.c_int]
     L.catmsm_profile_entries.restype = C.c_double
     L.catmsm_profile_entries.argtypes = []
     L.catmsm_profile_read.restype = C.c_int
@@ -242,3 +254,59 @@ def profile_read():
 
 def profile_entries() -> float:
     return load().catmsm_profile_entries()
+
+
+class Basis:
+    """A resident basis with fixed-base tables for batched commitments
+    (catmsm_basis_*; no reference counterpart)."""
+
+    def __init__(self, points: bytes, n: int, window: int = 0):
+        self.L = load()
+        self.n = n
+        self._pts = bytearray(points)
+        self.h = self.L.catmsm_basis_create(_buf(self._pts), n, window)
+        if not self.h:
+            raise RuntimeError("catmsm_basis_create failed")
+
+    def close(self):
+        if self.h:
+            self.L.catmsm_basis_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def config(self):
+        w, c = C.c_size_t(), C.c_size_t()
+        self.L.catmsm_basis_config(self.h, C.byref(w), C.byref(c))
+        return w.value, c.value
+
+    def set_config(self, window, chunk):
+        rc = self.L.catmsm_basis_set_config(self.h, window, chunk)
+        if rc != 0:
+            raise RuntimeError("catmsm_basis_set_config failed: %d" % rc)
+
+    def _args(self, counts, scalars):
+        cnt = (C.c_size_t * len(counts))(*counts)
+        sb = bytearray(scalars)
+        return cnt, sb
+
+    def msm_batch(self, counts, scalars: bytes, use_graph=True) -> bytes:
+        """counts[j] points per MSM; scalars: concatenated 32-byte scalars.
+        Returns len(counts) Jacobian blst_p1 (144 bytes each)."""
+        cnt, sb = self._args(counts, scalars)
+        out = bytearray(P1 * len(counts))
+        rc = self.L.catmsm_basis_msm_batch(self.h, _buf(out), len(counts), cnt, _buf(sb), 1 if use_graph else 0)
+        if rc != 0:
+            raise RuntimeError("catmsm_basis_msm_batch failed: %d" % rc)
+        return bytes(out)
+
+    def autotune(self, counts, scalars: bytes, force=False):
+        cnt, sb = self._args(counts, scalars)
+        rc = self.L.catmsm_basis_autotune(self.h, len(counts), cnt, _buf(sb), 1 if force else 0)
+        if rc != 0:
+            raise RuntimeError("catmsm_basis_autotune failed: %d" % rc)
+        return self.config()
