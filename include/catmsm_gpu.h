@@ -105,6 +105,17 @@ int catmsm_p1s_mult_pippenger_device(blst_p1 *ret, const void *d_points, const v
  * forward, 1: inverse (scaled), 2: inverse unscaled.  Returns 0 on success. */
 int catmsm_p1_fft_device(void *d_values, size_t n, const void *d_domain, int mode);
 
+/* A batch of G1 FFTs in one pass (no reference counterpart): transform i is
+ * blst_p1_fft_with_domain(values[i], ns[i], domains[i], ns[i] + 2, ...) with
+ * modes[i] = 0 forward, 1 inverse (scaled by domain[n]), 2 inverse unscaled
+ * (as blst_p1_ifft_unscaled_with_domain).  Sizes may differ; every stage
+ * level runs as one launch over all transforms that have it.  Any invalid
+ * entry (NULL values, bad size, domain length or tag, bad mode) returns
+ * cudaErrorInvalidValue before anything is written.  Host buffers; returns 0
+ * on success or a cudaError_t value (values untouched on failure). */
+int catmsm_p1_fft_batch(blst_p1 *const values[], const size_t ns[], const blst_fr *const domains[],
+                        const int modes[], size_t count);
+
 /* The calling thread's library CUDA stream (cudaStream_t), for event timing. */
 void *catmsm_stream(void);
 

@@ -62,6 +62,8 @@ def load(build_if_missing=True):
     L.catmsm_p1s_mult_pippenger_device.argtypes = [_vp, _vp, _vp, _sz, _sz, _sz, _sz]
     L.catmsm_p1_fft_device.restype = C.c_int
     L.catmsm_p1_fft_device.argtypes = [_vp, _sz, _vp, C.c_int]
+    L.catmsm_p1_fft_batch.restype = C.c_int
+    L.catmsm_p1_fft_batch.argtypes = [_vp, _vp, _vp, _vp, _sz]
     L.catmsm_stream.restype = _vp
     L.catmsm_stream.argtypes = []
     L.catmsm_launch_count.restype = C.c_long
@@ -178,6 +180,22 @@ def p1_ifft_unscaled_with_domain(values: bytes, n: int, domain: bytes, domain_le
     ok = load().blst_p1_ifft_unscaled_with_domain(_buf(b) if b else None, n, _buf(domain) if domain else None,
                                                   domain_len)
     return ok, bytes(b)
+
+
+def p1_fft_batch(values_list, ns, domains, modes):
+    """Batch of G1 FFTs; returns (rc, list of output byte strings)."""
+    L = load()
+    bufs = [bytearray(v) for v in values_list]
+    doms = [bytearray(d) for d in domains]
+    vb = [_buf(b) for b in bufs]
+    db = [_buf(d) for d in doms]
+    count = len(bufs)
+    varr = (C.c_void_p * count)(*[C.cast(x, C.c_void_p) for x in vb])
+    darr = (C.c_void_p * count)(*[C.cast(x, C.c_void_p) for x in db])
+    narr = (C.c_size_t * count)(*ns)
+    marr = (C.c_int * count)(*modes)
+    rc = L.catmsm_p1_fft_batch(varr, narr, darr, marr, count)
+    return rc, [bytes(b) for b in bufs]
 
 
 def points_from_scalars(k32: bytes, n: int) -> bytes:

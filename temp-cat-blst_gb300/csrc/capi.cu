@@ -13,6 +13,7 @@
 #include <climits>
 #include <cstring>
 #include <new>
+#include <vector>
 
 namespace catmsm {
 
@@ -261,6 +262,71 @@ bool blst_p1_ifft_unscaled_with_domain(blst_p1* values, size_t n, const blst_fr*
         return fft_entry(values, n, domain, true, false);
     } catch (...) {
         return false;
+    }
+}
+
+int catmsm_p1_fft_batch(blst_p1* const values[], const size_t ns[], const blst_fr* const domains[],
+                        const int modes[], size_t count)
+{
+    try {
+        if (!values || !ns || !domains || !modes) return (int)cudaErrorInvalidValue;
+        size_t total = 0;
+        for (size_t i = 0; i < count; i++) {
+            if (!values[i] || modes[i] < 0 || modes[i] > 2 || !domain_tag_ok(ns[i], domains[i], ns[i] + 2))
+                return (int)cudaErrorInvalidValue;
+            total += ns[i];
+        }
+        if (count == 0) return 0;
+        if (total >= 0x7fffffffu) return (int)cudaErrorInvalidValue;
+        Ctx* ctx = get_ctx();
+        if (!ctx) return (int)cudaErrorInitializationError;
+        cudaStream_t st = ctx->stream;
+        // distinct domains are uploaded once
+        std::vector<const blst_fr*> uniq;
+        std::vector<size_t> uoff, dom_of(count);
+        size_t rtot = 0;
+        for (size_t i = 0; i < count; i++) {
+            size_t u = 0;
+            while (u < uniq.size() && uniq[u] != domains[i]) u++;
+            if (u == uniq.size()) {
+                uniq.push_back(domains[i]);
+                uoff.push_back(rtot);
+                rtot += ns[i] + 1;
+            }
+            dom_of[i] = u;
+        }
+        blst_p1* dv = (blst_p1*)ctx->fft.values.get(total * sizeof(blst_p1));
+        uint32_t* dr = (uint32_t*)ctx->fft.roots.get(rtot * sizeof(blst_fr));
+        void* hstage = ctx->h_values.get(total * sizeof(blst_p1));
+        if (!dv || !dr || !hstage) return (int)cudaErrorMemoryAllocation;
+        cudaError_t err = cudaSuccess;
+        for (size_t u = 0; u < uniq.size() && err == cudaSuccess; u++) {
+            size_t n = 0;
+            for (size_t i = 0; i < count; i++)
+                if (domains[i] == uniq[u]) n = ns[i];
+            err = cudaMemcpyAsync(dr + 8 * uoff[u], uniq[u], (n + 1) * sizeof(blst_fr), cudaMemcpyHostToDevice, st);
+        }
+        std::vector<FftSpec> specs(count);
+        size_t off = 0;
+        for (size_t i = 0; i < count && err == cudaSuccess; i++) {
+            const uint32_t* r = dr + 8 * uoff[dom_of[i]];
+            specs[i] = FftSpec{ns[i], r, modes[i] != 0, modes[i] == 1 ? r + 8 * ns[i] : nullptr};
+            err = cudaMemcpyAsync(dv + off, values[i], ns[i] * sizeof(blst_p1), cudaMemcpyHostToDevice, st);
+            off += ns[i];
+        }
+        if (err == cudaSuccess) err = fft_run_multi(ctx, dv, specs.data(), count);
+        if (err == cudaSuccess)
+            err = cudaMemcpyAsync(hstage, dv, total * sizeof(blst_p1), cudaMemcpyDeviceToHost, st);
+        if (err == cudaSuccess) err = cudaStreamSynchronize(st);
+        if (err != cudaSuccess) return (int)err;
+        off = 0;
+        for (size_t i = 0; i < count; i++) {
+            std::memcpy(values[i], (const blst_p1*)hstage + off, ns[i] * sizeof(blst_p1));
+            off += ns[i];
+        }
+        return 0;
+    } catch (...) {
+        return (int)cudaErrorUnknown;
     }
 }
 

@@ -13,6 +13,19 @@ cudaError_t points_from_scalars_device(Ctx* ctx, const uint8_t* d_k32, size_t n,
 
 cudaError_t fp_mul_test_device(Ctx* ctx, const uint64_t* d_a, const uint64_t* d_b, uint64_t* d_out, size_t n);
 
+// One transform of a batch: n points, the n Montgomery roots its butterflies
+// index, whether the inverse reads forward roots at n - idx, and an optional
+// Montgomery scale applied to every output (all device pointers).
+struct FftSpec {
+    size_t n;
+    const uint32_t* roots_mont;
+    bool inv_from_fwd;
+    const uint32_t* scale_mont;
+};
+
+// Every transform of `specs` over the concatenated values in d_values.
+cudaError_t fft_run_multi(Ctx* ctx, void* d_values, const FftSpec* specs, size_t count);
+
 // G1 FFT over device-resident Jacobian values (blst_p1 layout).
 // d_roots_mont: the n Montgomery-form Fr roots the butterflies index;
 // inv_from_fwd: read index n - j*(n/len) (inverse from forward roots);

@@ -67,7 +67,7 @@ struct MsmWork {
 };
 
 struct FftWork {
-    DevBuf values, roots, glv, scratch;
+    DevBuf values, roots, glv, scratch, meta;
 };
 
 // Per-stage CUDA-event timing of the MSM pipeline (off by default).
@@ -85,7 +85,7 @@ struct Ctx {
     cudaStream_t stream = nullptr;
     MsmWork msm;
     FftWork fft;
-    PinnedBuf h_points, h_scalars, h_out, h_values;
+    PinnedBuf h_points, h_scalars, h_out, h_values, h_meta;
     StageProfile prof;
 };
 

@@ -7,15 +7,19 @@
 // (root j * n/len, or n - j * n/len when the inverse reads forward roots), so
 // outputs equal the reference's for any root table the caller supplies.
 //
-// Device layout: n Jacobian points (blst_p1 bytes, 144 B) in HBM.
-//   k_roots_prepare  per root index: Montgomery Fr -> canonical -> GLV halves
-//                    (k = k1 + lambda k2), stored as 8 words.
-//   k_bitrev         out-of-place bit-reversal permutation.
-//   k_fft_stage      one launch per stage; threads map first onto the
-//                    non-trivial butterflies (j >= 1, one GLV wNAF-5 scalar
-//                    multiplication each), then onto the j == 0 butterflies,
-//                    so a warp rarely mixes the two.
-//   k_fft_scale      inverse 1/n scale: one GLV multiplication per element.
+// Device layout: the Jacobian points (blst_p1 bytes, 144 B) of one or many
+// transforms, concatenated in HBM; a job descriptor per transform.
+//   k_roots_prepare    per root index: Montgomery Fr -> canonical -> GLV
+//                      halves (k = k1 + lambda k2), stored as 8 words.
+//   k_bitrev_multi     out-of-place bit-reversal permutation of every job.
+//   k_fft_stage_multi  one launch per stage level for ALL jobs that have the
+//                      level (a batch of transforms fills the GPU where one
+//                      small transform cannot); inside a job, threads map
+//                      first onto the non-trivial butterflies (j >= 1, one
+//                      GLV wNAF-5 scalar multiplication each), then onto the
+//                      j == 0 butterflies, so a warp rarely mixes the two.
+//   k_fft_finish_multi the inverse 1/n scale (one GLV multiplication per
+//                      element of scaled jobs) and canonical coordinates.
 // Each butterfly is ~1.7k Fp multiplications (~1M IMAD) against 576 bytes of
 // traffic, so the stages are IMAD-bound and read/write straight from HBM/L2;
 // staging tiles in shared memory would save nothing measurable.
@@ -23,6 +27,9 @@
 #include "curve.cuh"
 #include "fr.cuh"
 #include "catmsm_internal.h"
+
+#include <cstring>
+#include <vector>
 
 namespace catmsm {
 
@@ -67,68 +74,98 @@ __global__ void k_root_powers(const uint32_t* __restrict__ w, uint32_t n, uint32
     for (int k = 0; k < 8; k++) out[8 * i + k] = o[k];
 }
 
-__global__ void k_bitrev(const jac* __restrict__ in, jac* __restrict__ out, uint32_t n, uint32_t logn)
+// A batch of transforms shares one launch per stage level.  Job descriptor:
+struct FftJob {
+    uint32_t val_off;    // first element of this transform in the values buffer
+    uint32_t n, logn;
+    uint32_t glv_off;    // first prepared root (8 words each); glv_off + n: the scale
+    int32_t inv_from_fwd;
+    int32_t scaled;
+};
+
+// thread t of a launch over per-job ranges: find the job whose range holds t
+// (pre: exclusive prefix of the ranges, `cnt` entries; ids: job per entry)
+__device__ __forceinline__ uint32_t find_range(const uint32_t* __restrict__ pre, uint32_t cnt, uint32_t t)
 {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const uint32_t r = logn ? (__brev(i) >> (32 - logn)) : 0;
-    jac p;
-    load_jac(p, in + i);
-    store_jac(out + r, p);
+    uint32_t lo = 0, hi = cnt;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (pre[mid] <= t) lo = mid;
+        else hi = mid;
+    }
+    return lo;
 }
 
-__global__ void __launch_bounds__(128) k_fft_stage(jac* __restrict__ a, uint32_t n, uint32_t len,
-                                                   const uint32_t* __restrict__ glv, int inv_from_fwd)
+__global__ void k_bitrev_multi(const jac* __restrict__ in, jac* __restrict__ out, const FftJob* __restrict__ jobs,
+                               const uint32_t* __restrict__ pre, uint32_t njobs, uint32_t total)
 {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= total) return;
+    const FftJob J = jobs[find_range(pre, njobs, t)];
+    const uint32_t i = t - J.val_off;
+    const uint32_t r = J.logn ? (__brev(i) >> (32 - J.logn)) : 0;
+    jac p;
+    load_jac(p, in + t);
+    store_jac(out + J.val_off + r, p);
+}
+
+// Stage `len` over every job with n >= len.  lst: for this stage, pairs of
+// (job id, exclusive prefix of n/2 butterflies), `cnt` entries.
+__global__ void __launch_bounds__(64) k_fft_stage_multi(jac* __restrict__ a, const FftJob* __restrict__ jobs,
+                                                        const uint32_t* __restrict__ lst_job,
+                                                        const uint32_t* __restrict__ lst_pre, uint32_t cnt,
+                                                        uint32_t total, uint32_t len, const uint32_t* __restrict__ glv)
+{
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= total) return;
+    const uint32_t e = find_range(lst_pre, cnt, t);
+    const FftJob J = jobs[lst_job[e]];
+    const uint32_t b = t - lst_pre[e];
     const uint32_t half = len >> 1;
-    const uint32_t groups = n / len;
+    const uint32_t groups = J.n / len;
     const uint32_t nontriv = groups * (half - 1);
     uint32_t g, j;
-    if (t < nontriv) {
-        g = t / (half - 1);
-        j = 1 + t % (half - 1);
-    } else if (t < nontriv + groups) {
-        g = t - nontriv;
-        j = 0;
+    if (b < nontriv) {
+        g = b / (half - 1);
+        j = 1 + b % (half - 1);
     } else {
-        return;
+        g = b - nontriv;
+        j = 0;
     }
+    jac* base = a + J.val_off;
     const uint32_t i0 = g * len + j, i1 = i0 + half;
     jac u, v;
-    load_jac(u, a + i0);
-    load_jac(v, a + i1);
+    load_jac(u, base + i0);
+    load_jac(v, base + i1);
     if (j) {
-        uint32_t idx = j * (n / len);
-        if (inv_from_fwd) idx = n - idx;
-        jac_mult_glv(v, v, glv + 8 * idx, glv + 8 * idx + 4);
+        uint32_t idx = j * (J.n / len);
+        if (J.inv_from_fwd) idx = J.n - idx;
+        const uint32_t* r = glv + 8 * (size_t)(J.glv_off + idx);
+        jac_mult_glv(v, v, r, r + 4);
     }
     jac s = u;
     jac_add(s, v);
     jac_neg(v);
     jac_add(u, v);
-    store_jac(a + i0, s);
-    store_jac(a + i1, u);
+    store_jac(base + i0, s);
+    store_jac(base + i1, u);
 }
 
-__global__ void __launch_bounds__(128) k_fft_scale(jac* __restrict__ a, uint32_t n, const uint32_t* __restrict__ glv)
+// inverse scale (jobs with scaled != 0) and canonicalisation of every element
+__global__ void __launch_bounds__(64) k_fft_finish_multi(jac* __restrict__ a, const FftJob* __restrict__ jobs,
+                                                         const uint32_t* __restrict__ pre, uint32_t njobs,
+                                                         uint32_t total, const uint32_t* __restrict__ glv,
+                                                         int do_scale)
 {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= total) return;
+    const FftJob J = jobs[find_range(pre, njobs, t)];
     jac v;
-    load_jac(v, a + i);
-    jac_mult_glv(v, v, glv, glv + 4);
-    store_jac(a + i, v);
-}
-
-// Canonicalise coordinates to [0, p) so the output bytes are reduced
-// Montgomery values like the reference's.
-__global__ void k_canon(jac* __restrict__ a, uint32_t n)
-{
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    jac v;
-    load_jac(v, a + i);
+    load_jac(v, a + t);
+    if (do_scale && J.scaled) {
+        const uint32_t* r = glv + 8 * (size_t)(J.glv_off + J.n);
+        jac_mult_glv(v, v, r, r + 4);
+    }
     if (jac_is_inf(v)) {
         jac_set_inf(v);
     } else {
@@ -136,42 +173,104 @@ __global__ void k_canon(jac* __restrict__ a, uint32_t n)
         fp_canon(v.y, v.y);
         fp_canon(v.z, v.z);
     }
-    store_jac(a + i, v);
+    store_jac(a + t, v);
 }
 
-// d_values: n Jacobian points; d_roots_mont: n Montgomery roots (the table
-// the butterflies index); d_scale_mont: optional Montgomery scale factor.
-// The result lands back in d_values.
-cudaError_t fft_run(Ctx* ctx, void* d_values, size_t n, const uint32_t* d_roots_mont, bool inv_from_fwd,
-                    const uint32_t* d_scale_mont)
+// Runs every job of `specs` over the concatenated values in d_values
+// (job i at element offset sum_{j<i} n_j); results land back in d_values.
+cudaError_t fft_run_multi(Ctx* ctx, void* d_values, const FftSpec* specs, size_t count)
 {
     cudaStream_t st = ctx->stream;
     FftWork& W = ctx->fft;
-    jac* vals = (jac*)d_values;
-    jac* tmp = (jac*)W.scratch.get(n * sizeof(jac));
-    uint32_t* glv = (uint32_t*)W.glv.get((n + 1) * 32);
-    if (!tmp || !glv) return cudaErrorMemoryAllocation;
-    uint32_t logn = 0;
-    while (((size_t)1 << logn) < n) logn++;
-    k_roots_prepare<<<div_up(n, 256), 256, 0, st>>>(d_roots_mont, (uint32_t)n, glv);
-    if (d_scale_mont) k_roots_prepare<<<1, 32, 0, st>>>(d_scale_mont, 1, glv + 8 * n);
-    k_bitrev<<<div_up(n, 256), 256, 0, st>>>(vals, tmp, (uint32_t)n, logn);
-    g_stats.launches += 2 + (d_scale_mont ? 1 : 0);
-    for (size_t len = 2; len <= n; len <<= 1) {
-        const size_t half = len / 2, groups = n / len;
-        const size_t threads = groups * (half - 1) + groups;
-        k_fft_stage<<<div_up(threads, 128), 128, 0, st>>>(tmp, (uint32_t)n, (uint32_t)len, glv, inv_from_fwd ? 1 : 0);
+    std::vector<FftJob> jobs(count);
+    std::vector<uint32_t> vpre(count + 1);
+    size_t total = 0, glv_total = 0;
+    uint32_t maxlog = 0;
+    bool any_scale = false;
+    for (size_t i = 0; i < count; i++) {
+        const size_t n = specs[i].n;
+        uint32_t lg = 0;
+        while (((size_t)1 << lg) < n) lg++;
+        jobs[i].val_off = (uint32_t)total;
+        jobs[i].n = (uint32_t)n;
+        jobs[i].logn = lg;
+        jobs[i].inv_from_fwd = specs[i].inv_from_fwd ? 1 : 0;
+        jobs[i].scaled = specs[i].scale_mont ? 1 : 0;
+        jobs[i].glv_off = (uint32_t)glv_total;
+        vpre[i] = (uint32_t)total;
+        total += n;
+        glv_total += n + 1;
+        maxlog = lg > maxlog ? lg : maxlog;
+        any_scale |= specs[i].scale_mont != nullptr;
+    }
+    vpre[count] = (uint32_t)total;
+    if (total >= 0x7fffffffu) return cudaErrorInvalidValue;
+    // per-stage (job, prefix) lists
+    std::vector<uint32_t> lst_job, lst_pre, st_off(maxlog + 2), st_cnt(maxlog + 2), st_tot(maxlog + 2);
+    for (uint32_t s = 1; s <= maxlog; s++) {
+        st_off[s] = (uint32_t)lst_job.size();
+        uint32_t acc = 0;
+        for (size_t i = 0; i < count; i++) {
+            if (jobs[i].logn >= s) {
+                lst_job.push_back((uint32_t)i);
+                lst_pre.push_back(acc);
+                acc += jobs[i].n / 2;
+            }
+        }
+        st_cnt[s] = (uint32_t)lst_job.size() - st_off[s];
+        st_tot[s] = acc;
+    }
+    const size_t meta_words = count * (sizeof(FftJob) / 4) + (count + 1) + 2 * lst_job.size() + 8;
+    jac* tmp = (jac*)W.scratch.get(total * sizeof(jac));
+    uint32_t* glv = (uint32_t*)W.glv.get(glv_total * 32);
+    uint32_t* meta = (uint32_t*)W.meta.get(meta_words * 4);
+    uint32_t* hmeta = (uint32_t*)ctx->h_meta.get(meta_words * 4);
+    if (!tmp || !glv || !meta || !hmeta) return cudaErrorMemoryAllocation;
+    uint32_t* hp = hmeta;
+    std::memcpy(hp, jobs.data(), count * sizeof(FftJob));
+    hp += count * (sizeof(FftJob) / 4);
+    std::memcpy(hp, vpre.data(), (count + 1) * 4);
+    hp += count + 1;
+    if (!lst_job.empty()) {
+        std::memcpy(hp, lst_job.data(), lst_job.size() * 4);
+        std::memcpy(hp + lst_job.size(), lst_pre.data(), lst_pre.size() * 4);
+    }
+    CATMSM_CHECK(cudaMemcpyAsync(meta, hmeta, meta_words * 4, cudaMemcpyHostToDevice, st));
+    const FftJob* d_jobs = reinterpret_cast<const FftJob*>(meta);
+    const uint32_t* d_vpre = meta + count * (sizeof(FftJob) / 4);
+    const uint32_t* d_lst_job = d_vpre + count + 1;
+    const uint32_t* d_lst_pre = d_lst_job + lst_job.size();
+    // prepared roots per job (jobs sharing a root table share the work only
+    // through the L2; preparation is O(n) next to O(n log n) scalar mults)
+    for (size_t i = 0; i < count; i++) {
+        k_roots_prepare<<<div_up(jobs[i].n, 256), 256, 0, st>>>(specs[i].roots_mont, jobs[i].n, glv + 8 * (size_t)jobs[i].glv_off);
+        if (specs[i].scale_mont)
+            k_roots_prepare<<<1, 32, 0, st>>>(specs[i].scale_mont, 1, glv + 8 * (size_t)(jobs[i].glv_off + jobs[i].n));
+        g_stats.launches += 1 + (specs[i].scale_mont ? 1 : 0);
+    }
+    k_bitrev_multi<<<div_up(total, 256), 256, 0, st>>>((const jac*)d_values, tmp, d_jobs, d_vpre, (uint32_t)count,
+                                                       (uint32_t)total);
+    g_stats.launches++;
+    for (uint32_t s = 1; s <= maxlog; s++) {
+        k_fft_stage_multi<<<div_up(st_tot[s], 64), 64, 0, st>>>(tmp, d_jobs, d_lst_job + st_off[s], d_lst_pre + st_off[s],
+                                                                st_cnt[s], st_tot[s], 1u << s, glv);
         g_stats.launches++;
     }
-    if (d_scale_mont) {
-        k_fft_scale<<<div_up(n, 128), 128, 0, st>>>(tmp, (uint32_t)n, glv + 8 * n);
-        g_stats.launches++;
-    }
-    k_canon<<<div_up(n, 256), 256, 0, st>>>(tmp, (uint32_t)n);
+    k_fft_finish_multi<<<div_up(total, 64), 64, 0, st>>>(tmp, d_jobs, d_vpre, (uint32_t)count, (uint32_t)total, glv,
+                                                         any_scale ? 1 : 0);
     g_stats.launches++;
     CATMSM_CHECK(cudaGetLastError());
-    CATMSM_CHECK(cudaMemcpyAsync(vals, tmp, n * sizeof(jac), cudaMemcpyDeviceToDevice, st));
+    CATMSM_CHECK(cudaMemcpyAsync(d_values, tmp, total * sizeof(jac), cudaMemcpyDeviceToDevice, st));
     return cudaSuccess;
+}
+
+// single transform: d_values n Jacobian points; d_roots_mont the n
+// Montgomery roots the butterflies index; d_scale_mont optional scale
+cudaError_t fft_run(Ctx* ctx, void* d_values, size_t n, const uint32_t* d_roots_mont, bool inv_from_fwd,
+                    const uint32_t* d_scale_mont)
+{
+    FftSpec sp{n, d_roots_mont, inv_from_fwd, d_scale_mont};
+    return fft_run_multi(ctx, d_values, &sp, 1);
 }
 
 cudaError_t fft_root_powers(Ctx* ctx, const uint32_t* d_w_mont, size_t n, uint32_t* d_out)

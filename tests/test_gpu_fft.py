@@ -109,3 +109,37 @@ def test_fft_matches_oracle_arbitrary_domain_values(gpu, oracle):
         assert ok and ok2
         for i in range(n):
             assert oracle.serialize(g[144 * i:144 * i + 144]) == oracle.serialize(o[144 * i:144 * i + 144])
+
+
+def test_fft_batch_matches_golden(gpu, oracle, golden):
+    """Every golden FFT case (sizes 1..4096, all five modes) in ONE batch."""
+    vals, ns, doms, modes, cases = [], [], [], [], []
+    mode_of = {"dfwd": 0, "dinv": 1, "dunscaled": 2}
+    for c in golden["fft"]:
+        if c["mode"] not in mode_of:
+            continue
+        n = c["n"]
+        aff = oracle.gen_points(c["seed"], n)
+        vals.append(oracle.jacobian_randomize(c["seed"], n, aff))
+        ns.append(n)
+        doms.append(gpu.fr_fft_domain_init(n)[1])
+        modes.append(mode_of[c["mode"]])
+        cases.append(c)
+    rc, outs = gpu.p1_fft_batch(vals, ns, doms, modes)
+    assert rc == 0
+    for c, out in zip(cases, outs):
+        n = c["n"]
+        ser = b"".join(oracle.serialize(out[144 * i:144 * i + 144]) for i in range(n))
+        assert hashlib.sha256(ser).hexdigest() == c["sha256"], (n, c["mode"])
+
+
+def test_fft_batch_rejects_before_writing(gpu, oracle):
+    n = 8
+    jac = oracle.jacobian_randomize(9, n, oracle.gen_points(9, n))
+    d = gpu.fr_fft_domain_init(n)[1]
+    bad = bytearray(d)
+    bad[-1] ^= 1
+    rc, outs = gpu.p1_fft_batch([jac, jac], [n, n], [d, bytes(bad)], [0, 0])
+    assert rc != 0 and outs == [jac, jac]
+    rc, outs = gpu.p1_fft_batch([jac], [n], [d], [3])
+    assert rc != 0 and outs == [jac]
