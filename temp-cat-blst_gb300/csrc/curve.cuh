@@ -267,59 +267,59 @@ __device__ __constant__ static const uint32_t FP_BETA[12] = {
     0x8671f071u, 0xcd03c9e4u, 0x1fcda5d2u, 0x5dab2246u, 0xd3851b95u, 0x587042afu,
     0x01bacb9eu, 0x8eb60ebeu, 0x83d050d2u, 0x03f97d6eu, 0x54638741u, 0x18f02065u};
 
-// width-5 NAF digits of a 128-bit value (4 little-endian words); returns length
-__device__ __forceinline__ int wnaf5_128(int8_t* d, const uint32_t* kin)
+// Signed fixed-window digits of a 128-bit value (4 little-endian words):
+// 33 digits d_i in [-8, 8] with value = sum_i d_i 16^i (window recoding with
+// carry, as the MSM's digit recoding).  Every value uses the same 33 windows,
+// so lanes of a warp working on different scalars add at the same positions.
+__device__ __forceinline__ void booth4_128(int8_t* d, const uint32_t* k)
 {
-    uint32_t k[5] = {kin[0], kin[1], kin[2], kin[3], 0};
-    int len = 0;
-    while ((k[0] | k[1] | k[2] | k[3] | k[4]) != 0) {
-        int v = 0;
-        if (k[0] & 1) {
-            v = (int)(k[0] & 31);
-            if (v >= 16) v -= 32;
-            if (v > 0) {
-                uint32_t b = (uint32_t)v;
-                for (int i = 0; i < 5 && b; i++) { uint32_t o = k[i]; k[i] -= b; b = o < b; }
-            } else {
-                uint32_t cy = (uint32_t)(-v);
-                for (int i = 0; i < 5 && cy; i++) { k[i] += cy; cy = k[i] < cy; }
-            }
-        }
-        d[len++] = (int8_t)v;
-        for (int i = 0; i < 4; i++) k[i] = (k[i] >> 1) | (k[i + 1] << 31);
-        k[4] >>= 1;
+    uint32_t carry = 0;
+#pragma unroll
+    for (int i = 0; i < 33; i++) {
+        const uint32_t raw = i < 32 ? (k[i >> 3] >> (4 * (i & 7))) & 15u : 0u;
+        int v = (int)(raw + carry);
+        if (v > 8) { v -= 16; carry = 1; }
+        else carry = 0;
+        d[i] = (int8_t)v;
     }
-    return len;
 }
 
-// out = (k1 + lambda k2) P for 128-bit k1, k2 (GLV + interleaved wNAF-5).
-// P must be in the prime-order subgroup (as the FFT contract requires).
+// out = (k1 + lambda k2) P for 128-bit k1, k2: GLV split with both halves in
+// signed 4-bit windows over one table {P, 2P, ..., 8P}; the k2 half uses
+// phi(T) = (beta X, Y, Z).  128 doublings + 66 additions, identical control
+// flow for every lane.  P must be in the prime-order subgroup (as the FFT
+// contract requires).
 static __device__ __noinline__ void jac_mult_glv(jac& out, const jac& P, const uint32_t* k1, const uint32_t* k2)
 {
-    int8_t d1[132], d2[132];
-    const int l1 = wnaf5_128(d1, k1);
-    const int l2 = wnaf5_128(d2, k2);
-    jac T[8];
+    int8_t d1[33], d2[33];
+    booth4_128(d1, k1);
+    booth4_128(d2, k2);
+    jac T[8];                                    // T[i] = (i + 1) P
     T[0] = P;
-    jac P2 = P;
-    jac_dbl(P2);
-    for (int i = 1; i < 8; i++) { T[i] = T[i - 1]; jac_add(T[i], P2); }
+    T[1] = P; jac_dbl(T[1]);
+    T[2] = T[1]; jac_add(T[2], P);
+    T[3] = T[1]; jac_dbl(T[3]);
+    T[4] = T[3]; jac_add(T[4], P);
+    T[5] = T[2]; jac_dbl(T[5]);
+    T[6] = T[5]; jac_add(T[6], P);
+    T[7] = T[3]; jac_dbl(T[7]);
     fp beta;
 #pragma unroll
     for (int i = 0; i < 12; i++) beta.v[i] = FP_BETA[i];
     jac acc;
     jac_set_inf(acc);
-    for (int i = (l1 > l2 ? l1 : l2) - 1; i >= 0; i--) {
-        jac_dbl(acc);
-        const int a = i < l1 ? d1[i] : 0;
-        const int b = i < l2 ? d2[i] : 0;
+    for (int i = 32; i >= 0; i--) {
+        if (i < 32) {
+            jac_dbl(acc); jac_dbl(acc); jac_dbl(acc); jac_dbl(acc);
+        }
+        const int a = d1[i], b = d2[i];
         if (a) {
-            jac t = T[(a > 0 ? a : -a) >> 1];
+            jac t = T[(a > 0 ? a : -a) - 1];
             if (a < 0) jac_neg(t);
             jac_add(acc, t);
         }
         if (b) {
-            jac t = T[(b > 0 ? b : -b) >> 1];
+            jac t = T[(b > 0 ? b : -b) - 1];
             fp_mul(t.x, t.x, beta);
             if (b < 0) jac_neg(t);
             jac_add(acc, t);

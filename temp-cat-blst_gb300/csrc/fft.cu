@@ -16,7 +16,8 @@
 //                      level (a batch of transforms fills the GPU where one
 //                      small transform cannot); inside a job, threads map
 //                      first onto the non-trivial butterflies (j >= 1, one
-//                      GLV wNAF-5 scalar multiplication each), then onto the
+//                      GLV scalar multiplication in signed 4-bit windows
+//                      each), then onto the
 //                      j == 0 butterflies, so a warp rarely mixes the two.
 //   k_fft_finish_multi the inverse 1/n scale (one GLV multiplication per
 //                      element of scaled jobs) and canonical coordinates.
