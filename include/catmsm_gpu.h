@@ -195,6 +195,30 @@ int catmsm_basis_msm_batch(void *basis, blst_p1 *out, size_t nmsm, const size_t 
                            const blst_byte *scalars, int use_graph);
 int catmsm_basis_autotune(void *basis, size_t nmsm, const size_t *counts, const blst_byte *scalars, int force);
 
+/* ---- Serving engine (no reference counterpart): continuous batching of MSM
+ * and FFT requests over a resident basis (catmsm_basis_create) on one GPU.
+ * `workers` threads each own a stream and a workspace; a free worker takes
+ * the queued requests at the head of the queue as one batch (all queued MSMs,
+ * or all queued FFTs, up to a point cap), so requests that arrive while other
+ * batches run join at the next batch boundary and batches of different
+ * workers overlap on the device.  A batch starts only while the estimated
+ * device memory of all in-flight batches stays within hbm_budget_bytes (0 =
+ * 64 GiB; a single request above the budget runs alone).
+ * submit_msm: MSM over the first k basis points with k 32-byte scalars;
+ * submit_fft: blst_p1_fft_with_domain semantics with mode 0 forward, 1 inverse,
+ * 2 inverse unscaled, in place on `values`.  Input buffers must stay valid
+ * until wait returns.  Both return a ticket (> 0) or -1 on invalid input.
+ * wait blocks until the ticket completes, writes the MSM result (Jacobian) to
+ * msm_out if not NULL and times_ms[0..1] = queueing and total latency in ms
+ * (host steady clock) if not NULL, and returns 0 or a cudaError_t value.
+ * The basis must not be reconfigured or destroyed while a server uses it. */
+void *catmsm_server_create(void *basis, size_t workers, size_t hbm_budget_bytes);
+void catmsm_server_destroy(void *server);
+int64_t catmsm_server_submit_msm(void *server, const blst_byte *scalars, size_t k);
+int64_t catmsm_server_submit_fft(void *server, blst_p1 *values, size_t n, const blst_fr *domain, int mode);
+int catmsm_server_wait(void *server, int64_t ticket, blst_p1 *msm_out, double *times_ms);
+int catmsm_server_stats(void *server, long *batches, long *batched_requests, long *max_batch);
+
 /* Field self-check: out[i] = a[i] * b[i] * R^-1 mod p (canonical), host
  * buffers of n blst_fp.  Returns 0 on success. */
 int catmsm_fp_mul(blst_fp *out, const blst_fp *a, const blst_fp *b, size_t n);

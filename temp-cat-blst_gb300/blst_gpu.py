@@ -96,6 +96,18 @@ def load(build_if_missing=True):
     L.catmsm_basis_msm_batch.argtypes = [_vp, _vp, _sz, _vp, _vp, C.c_int]
     L.catmsm_basis_autotune.restype = C.c_int
     L.catmsm_basis_autotune.argtypes = [_vp, _sz, _vp, _vp, C.c_int]
+    L.catmsm_server_create.restype = C.c_void_p
+    L.catmsm_server_create.argtypes = [_vp, _sz, _sz]
+    L.catmsm_server_destroy.restype = None
+    L.catmsm_server_destroy.argtypes = [_vp]
+    L.catmsm_server_submit_msm.restype = C.c_int64
+    L.catmsm_server_submit_msm.argtypes = [_vp, _vp, _sz]
+    L.catmsm_server_submit_fft.restype = C.c_int64
+    L.catmsm_server_submit_fft.argtypes = [_vp, _vp, _sz, _vp, C.c_int]
+    L.catmsm_server_wait.restype = C.c_int
+    L.catmsm_server_wait.argtypes = [_vp, C.c_int64, _vp, _vp]
+    L.catmsm_server_stats.restype = C.c_int
+    L.catmsm_server_stats.argtypes = [_vp, _vp, _vp, _vp]
     L.catmsm_profile_entries.restype = C.c_double
     L.catmsm_profile_entries.argtypes = []
     L.catmsm_profile_read.restype = C.c_int
@@ -328,3 +340,60 @@ class Basis:
         if rc != 0:
             raise RuntimeError("catmsm_basis_autotune failed: %d" % rc)
         return self.config()
+
+
+class Server:
+    """Continuous-batching request engine over a resident Basis
+    (catmsm_server_*; no reference counterpart).  Submitted buffers are kept
+    alive here until their ticket is waited on."""
+
+    def __init__(self, basis: "Basis", workers: int = 4, hbm_budget: int = 0):
+        self.L = load()
+        self.basis = basis
+        self.h = self.L.catmsm_server_create(basis.h, workers, hbm_budget)
+        if not self.h:
+            raise RuntimeError("catmsm_server_create failed")
+        self._keep = {}
+
+    def close(self):
+        if self.h:
+            self.L.catmsm_server_destroy(self.h)
+            self.h = None
+            self._keep.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit_msm(self, scalars: bytes, k: int) -> int:
+        buf = (C.c_char * len(scalars)).from_buffer_copy(scalars)
+        t = self.L.catmsm_server_submit_msm(self.h, buf, k)
+        if t < 0:
+            raise ValueError("submit_msm rejected")
+        self._keep[t] = (buf,)
+        return t
+
+    def submit_fft(self, values: bytes, n: int, domain: bytes, mode: int) -> int:
+        vb = (C.c_char * len(values)).from_buffer_copy(values)
+        db = (C.c_char * len(domain)).from_buffer_copy(domain)
+        t = self.L.catmsm_server_submit_fft(self.h, vb, n, db, mode)
+        if t < 0:
+            raise ValueError("submit_fft rejected")
+        self._keep[t] = (vb, db)
+        return t
+
+    def wait(self, ticket: int):
+        """(status, result bytes (MSM: 144-B Jacobian; FFT: the values), queue_ms, latency_ms)."""
+        out = (C.c_char * P1)()
+        times = (C.c_double * 2)()
+        rc = self.L.catmsm_server_wait(self.h, ticket, out, times)
+        keep = self._keep.pop(ticket)
+        res = bytes(keep[0]) if len(keep) == 2 else bytes(out)
+        return rc, res, times[0], times[1]
+
+    def stats(self):
+        a, b, c = C.c_long(), C.c_long(), C.c_long()
+        self.L.catmsm_server_stats(self.h, C.byref(a), C.byref(b), C.byref(c))
+        return {"batches": a.value, "requests": b.value, "max_batch": c.value}

@@ -204,17 +204,37 @@ struct BatchGraph {
     size_t cap = 0;
 };
 
+// Device/pinned workspace of one batch pipeline instance (a basis has one;
+// a server worker has its own, sharing the basis tables).
+struct BatchWork {
+    DevBuf scal, off, digits, ranks, pidx, counts, offsets, bsums, sorted_pt, sorted_key, buckets, head, tail,
+        hot, seg, out;
+    PinnedBuf h_scal, h_off, h_out;
+    BatchGraph graph;
+    void release()
+    {
+        if (graph.exec) cudaGraphExecDestroy(graph.exec);
+        graph = BatchGraph();
+        DevBuf* bufs[] = {&scal, &off, &digits, &ranks, &pidx, &counts, &offsets, &bsums, &sorted_pt,
+                          &sorted_key, &buckets, &head, &tail, &hot, &seg, &out};
+        for (DevBuf* d : bufs) d->release();
+        PinnedBuf* hb[] = {&h_scal, &h_off, &h_out};
+        for (PinnedBuf* h : hb) {
+            if (h->p) cudaFreeHost(h->p);
+            h->p = nullptr;
+            h->cap = 0;
+        }
+    }
+};
+
 struct Basis {
     int device = -1;
     size_t n = 0;
     uint32_t c = 0, D = 0, L = 16;
     cudaStream_t stream = nullptr;
     DevBuf points, table, tmp;
-    DevBuf scal, off, digits, ranks, pidx, counts, offsets, bsums, sorted_pt, sorted_key, buckets, head, tail,
-        hot, seg, out;
-    PinnedBuf h_scal, h_off, h_out;
-    BatchGraph graph;
-    size_t launches = 0;
+    BatchWork work;
+    std::mutex mu;     // serialises table rebuilds against running batches
 };
 
 static cudaError_t build_tables(Basis* b, uint32_t c)
@@ -230,15 +250,15 @@ static cudaError_t build_tables(Basis* b, uint32_t c)
     b->tmp.release();
     b->c = c;
     b->D = D;
-    if (b->graph.exec) {
-        cudaGraphExecDestroy(b->graph.exec);
-        b->graph = BatchGraph();
+    if (b->work.graph.exec) {
+        cudaGraphExecDestroy(b->work.graph.exec);
+        b->work.graph = BatchGraph();
     }
     return cudaSuccess;
 }
 
 // Workspace for batches of up to nmsm MSMs and cap pairs.
-static cudaError_t ensure_work(Basis* b, uint32_t nmsm, size_t cap)
+static cudaError_t ensure_work(const Basis* b, BatchWork* w, uint32_t nmsm, size_t cap)
 {
     const uint32_t B = 1u << (b->c - 1);
     const size_t M = (size_t)nmsm * B;
@@ -246,21 +266,20 @@ static cudaError_t ensure_work(Basis* b, uint32_t nmsm, size_t cap)
     const size_t chunks = (nD + b->L - 1) / b->L + 1;
     const size_t lvl1 = (size_t)nmsm * ((B + 7) / 8);
     const size_t lvl2 = (size_t)nmsm * ((B + 15) / 16) + nmsm;
-    bool ok = b->scal.get(cap * 32) && b->off.get((nmsm + 1) * 4) && b->digits.get(nD * 4) &&
-              b->ranks.get(nD * 4) && b->pidx.get(nD * 4) && b->counts.get(M * 4) && b->offsets.get((M + 1) * 4) &&
-              b->bsums.get(((M + kScanTileB - 1) / kScanTileB) * 4 + 4) && b->sorted_pt.get(nD * 4) &&
-              b->sorted_key.get(nD * 4) && b->buckets.get(M * sizeof(xyzz)) &&
-              b->head.get(chunks * sizeof(xyzz)) && b->tail.get(chunks * sizeof(xyzz)) &&
-              b->hot.get(256 + chunks * sizeof(uint2)) && b->seg.get(2 * (lvl1 + lvl2) * sizeof(xyzz)) &&
-              b->out.get((size_t)nmsm * sizeof(jac)) && b->h_scal.get(cap * 32) && b->h_off.get((nmsm + 1) * 4) &&
-              b->h_out.get((size_t)nmsm * sizeof(jac));
+    bool ok = w->scal.get(cap * 32) && w->off.get((nmsm + 1) * 4) && w->digits.get(nD * 4) &&
+              w->ranks.get(nD * 4) && w->pidx.get(nD * 4) && w->counts.get(M * 4) && w->offsets.get((M + 1) * 4) &&
+              w->bsums.get(((M + kScanTileB - 1) / kScanTileB) * 4 + 4) && w->sorted_pt.get(nD * 4) &&
+              w->sorted_key.get(nD * 4) && w->buckets.get(M * sizeof(xyzz)) &&
+              w->head.get(chunks * sizeof(xyzz)) && w->tail.get(chunks * sizeof(xyzz)) &&
+              w->hot.get(256 + chunks * sizeof(uint2)) && w->seg.get(2 * (lvl1 + lvl2) * sizeof(xyzz)) &&
+              w->out.get((size_t)nmsm * sizeof(jac)) && w->h_scal.get(cap * 32) && w->h_off.get((nmsm + 1) * 4) &&
+              w->h_out.get((size_t)nmsm * sizeof(jac));
     return ok ? cudaSuccess : cudaErrorMemoryAllocation;
 }
 
 // The device sequence of one batch (everything after the input copies).
-static void enqueue_batch(Basis* b, uint32_t nmsm, size_t cap)
+static void enqueue_batch(const Basis* b, BatchWork* w, cudaStream_t st, uint32_t nmsm, size_t cap)
 {
-    cudaStream_t st = b->stream;
     const uint32_t c = b->c, D = b->D, L = b->L, B = 1u << (c - 1);
     const size_t M = (size_t)nmsm * B;
     const size_t nD = cap * D;
@@ -268,33 +287,33 @@ static void enqueue_batch(Basis* b, uint32_t nmsm, size_t cap)
     const uint32_t nblocks = (uint32_t)((M + kScanTileB - 1) / kScanTileB);
     const size_t lvl1 = (size_t)nmsm * ((B + 7) / 8);
     const size_t lvl2 = (size_t)nmsm * ((B + 15) / 16) + nmsm;
-    uint32_t* off = (uint32_t*)b->off.p;
-    uint32_t* counts = (uint32_t*)b->counts.p;
-    uint32_t* offsets = (uint32_t*)b->offsets.p;
+    uint32_t* off = (uint32_t*)w->off.p;
+    uint32_t* counts = (uint32_t*)w->counts.p;
+    uint32_t* offsets = (uint32_t*)w->offsets.p;
     uint32_t* total = offsets + M;
-    uint32_t* hot_count = (uint32_t*)b->hot.p;
+    uint32_t* hot_count = (uint32_t*)w->hot.p;
     uint2* hot_list = reinterpret_cast<uint2*>(hot_count + 64);
-    xyzz* buckets = (xyzz*)b->buckets.p;
-    xyzz* head = (xyzz*)b->head.p;
-    xyzz* tail = (xyzz*)b->tail.p;
-    xyzz* seg = (xyzz*)b->seg.p;
+    xyzz* buckets = (xyzz*)w->buckets.p;
+    xyzz* head = (xyzz*)w->head.p;
+    xyzz* tail = (xyzz*)w->tail.p;
+    xyzz* seg = (xyzz*)w->seg.p;
     cudaMemsetAsync(counts, 0, M * 4, st);
     cudaMemsetAsync(buckets, 0, M * sizeof(xyzz), st);
     cudaMemsetAsync(hot_count, 0, 4, st);
-    k_digits_batch<<<div_up(cap, 256), 256, 0, st>>>((const uint8_t*)b->scal.p, off, nmsm, (uint32_t)b->n, 256, c,
-                                                    D, (uint32_t)cap, (uint32_t*)b->digits.p,
-                                                    (uint32_t*)b->ranks.p, (uint32_t*)b->pidx.p, counts);
-    k_scan_local<<<nblocks, 1024, 0, st>>>(counts, offsets, (uint32_t*)b->bsums.p, (uint32_t)M);
-    k_scan_top<<<1, 1024, 0, st>>>((uint32_t*)b->bsums.p, nblocks, total);
-    k_scan_add<<<div_up(M, 256), 256, 0, st>>>(offsets, (uint32_t*)b->bsums.p, (uint32_t)M);
-    k_scatter_batch<<<div_up(nD, 256), 256, 0, st>>>((const uint32_t*)b->digits.p, (const uint32_t*)b->ranks.p,
-                                                    (const uint32_t*)b->pidx.p, offsets, off, nmsm, D,
-                                                    (uint32_t)nD, (uint32_t*)b->sorted_pt.p,
-                                                    (uint32_t*)b->sorted_key.p);
-    k_accumulate<<<div_up(chunks, 128), 128, 0, st>>>((const affine*)b->table.p, (const uint32_t*)b->sorted_pt.p,
-                                                      (const uint32_t*)b->sorted_key.p, total, L, buckets, head,
+    k_digits_batch<<<div_up(cap, 256), 256, 0, st>>>((const uint8_t*)w->scal.p, off, nmsm, (uint32_t)b->n, 256, c,
+                                                    D, (uint32_t)cap, (uint32_t*)w->digits.p,
+                                                    (uint32_t*)w->ranks.p, (uint32_t*)w->pidx.p, counts);
+    k_scan_local<<<nblocks, 1024, 0, st>>>(counts, offsets, (uint32_t*)w->bsums.p, (uint32_t)M);
+    k_scan_top<<<1, 1024, 0, st>>>((uint32_t*)w->bsums.p, nblocks, total);
+    k_scan_add<<<div_up(M, 256), 256, 0, st>>>(offsets, (uint32_t*)w->bsums.p, (uint32_t)M);
+    k_scatter_batch<<<div_up(nD, 256), 256, 0, st>>>((const uint32_t*)w->digits.p, (const uint32_t*)w->ranks.p,
+                                                    (const uint32_t*)w->pidx.p, offsets, off, nmsm, D,
+                                                    (uint32_t)nD, (uint32_t*)w->sorted_pt.p,
+                                                    (uint32_t*)w->sorted_key.p);
+    k_accumulate<<<div_up(chunks, 128), 128, 0, st>>>((const affine*)b->table.p, (const uint32_t*)w->sorted_pt.p,
+                                                      (const uint32_t*)w->sorted_key.p, total, L, buckets, head,
                                                       tail);
-    k_fixup<<<div_up(chunks, 128), 128, 0, st>>>((const uint32_t*)b->sorted_key.p, offsets, total, L, buckets, head,
+    k_fixup<<<div_up(chunks, 128), 128, 0, st>>>((const uint32_t*)w->sorted_key.p, offsets, total, L, buckets, head,
                                                  tail, hot_list, hot_count);
     k_fixup_hot<<<2 * kSMs, 128, 0, st>>>(hot_list, hot_count, offsets, L, buckets, head, tail);
     xyzz* bufA[2] = {seg, seg + 2 * lvl1};
@@ -314,11 +333,14 @@ static void enqueue_batch(Basis* b, uint32_t nmsm, size_t cap)
         m = m_out;
         first = false;
     }
-    k_batch_out<<<div_up(nmsm, 128), 128, 0, st>>>(inQ ? inQ : inA, nmsm, (jac*)b->out.p);
+    k_batch_out<<<div_up(nmsm, 128), 128, 0, st>>>(inQ ? inQ : inA, nmsm, (jac*)w->out.p);
 }
 
-static cudaError_t run_batch(Basis* b, blst_p1* out, uint32_t nmsm, const size_t* counts, const uint8_t* scalars,
-                             bool use_graph)
+// exact_cap: size the work for exactly the pairs of this batch (serving);
+// otherwise for full-basis MSMs, so one captured graph serves every batch of
+// the same size.
+static cudaError_t run_batch(Basis* b, BatchWork* w, cudaStream_t st, blst_p1* out, uint32_t nmsm,
+                             const size_t* counts, const uint8_t* scalars, bool use_graph, bool exact_cap)
 {
     std::vector<uint32_t> off(nmsm + 1);
     size_t P = 0;
@@ -328,22 +350,21 @@ static cudaError_t run_batch(Basis* b, blst_p1* out, uint32_t nmsm, const size_t
         P += counts[j];
     }
     off[nmsm] = (uint32_t)P;
-    const size_t cap = (size_t)nmsm * b->n;          // graph shapes are sized for full MSMs
+    const size_t cap = exact_cap ? (P ? P : 1) : (size_t)nmsm * b->n;
     if (cap * b->D >= 0x7fffffffu) return cudaErrorInvalidValue;
-    CATMSM_CHECK(ensure_work(b, nmsm, cap));
-    std::memcpy(b->h_scal.p, scalars, P * 32);
-    std::memcpy(b->h_off.p, off.data(), (nmsm + 1) * 4);
-    cudaStream_t st = b->stream;
-    CATMSM_CHECK(cudaMemcpyAsync(b->scal.p, b->h_scal.p, P * 32, cudaMemcpyHostToDevice, st));
-    CATMSM_CHECK(cudaMemcpyAsync(b->off.p, b->h_off.p, (nmsm + 1) * 4, cudaMemcpyHostToDevice, st));
+    CATMSM_CHECK(ensure_work(b, w, nmsm, cap));
+    std::memcpy(w->h_scal.p, scalars, P * 32);
+    std::memcpy(w->h_off.p, off.data(), (nmsm + 1) * 4);
+    CATMSM_CHECK(cudaMemcpyAsync(w->scal.p, w->h_scal.p, P * 32, cudaMemcpyHostToDevice, st));
+    CATMSM_CHECK(cudaMemcpyAsync(w->off.p, w->h_off.p, (nmsm + 1) * 4, cudaMemcpyHostToDevice, st));
     if (use_graph) {
-        BatchGraph& g = b->graph;
+        BatchGraph& g = w->graph;
         if (!g.exec || g.nmsm != nmsm || g.c != b->c || g.L != b->L || g.cap != cap) {
             if (g.exec) cudaGraphExecDestroy(g.exec);
             g = BatchGraph();
             cudaGraph_t graph;
             CATMSM_CHECK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-            enqueue_batch(b, nmsm, cap);
+            enqueue_batch(b, w, st, nmsm, cap);
             CATMSM_CHECK(cudaStreamEndCapture(st, &graph));
             cudaError_t e = cudaGraphInstantiate(&g.exec, graph, 0);
             cudaGraphDestroy(graph);
@@ -356,15 +377,34 @@ static cudaError_t run_batch(Basis* b, blst_p1* out, uint32_t nmsm, const size_t
         CATMSM_CHECK(cudaGraphLaunch(g.exec, st));
         g_stats.launches += 1;
     } else {
-        enqueue_batch(b, nmsm, cap);
+        enqueue_batch(b, w, st, nmsm, cap);
         g_stats.launches += 12;
     }
     CATMSM_CHECK(cudaGetLastError());
-    CATMSM_CHECK(cudaMemcpyAsync(b->h_out.p, b->out.p, (size_t)nmsm * sizeof(jac), cudaMemcpyDeviceToHost, st));
+    CATMSM_CHECK(cudaMemcpyAsync(w->h_out.p, w->out.p, (size_t)nmsm * sizeof(jac), cudaMemcpyDeviceToHost, st));
     CATMSM_CHECK(cudaStreamSynchronize(st));
-    std::memcpy(out, b->h_out.p, (size_t)nmsm * sizeof(jac));
+    std::memcpy(out, w->h_out.p, (size_t)nmsm * sizeof(jac));
     return cudaSuccess;
 }
+
+BatchWork* batch_work_new() { return new (std::nothrow) BatchWork(); }
+
+void batch_work_free(BatchWork* w)
+{
+    if (!w) return;
+    w->release();
+    delete w;
+}
+
+cudaError_t batch_run(Basis* b, BatchWork* w, cudaStream_t st, blst_p1* out, uint32_t nmsm, const size_t* counts,
+                      const uint8_t* scalars)
+{
+    return run_batch(b, w, st, out, nmsm, counts, scalars, false, true);
+}
+
+size_t basis_points(const Basis* b) { return b->n; }
+uint32_t basis_window(const Basis* b) { return b->c; }
+int basis_device(const Basis* b) { return b->device; }
 
 // ---------------------------------------------------------------- autotune cache
 static std::mutex g_tune_mu;
@@ -459,14 +499,10 @@ void catmsm_basis_destroy(void* handle)
 {
     Basis* b = (Basis*)handle;
     if (!b) return;
-    if (b->graph.exec) cudaGraphExecDestroy(b->graph.exec);
-    DevBuf* bufs[] = {&b->points, &b->table, &b->tmp, &b->scal, &b->off, &b->digits, &b->ranks, &b->pidx,
-                      &b->counts, &b->offsets, &b->bsums, &b->sorted_pt, &b->sorted_key, &b->buckets,
-                      &b->head, &b->tail, &b->hot, &b->seg, &b->out};
-    for (DevBuf* d : bufs) d->release();
-    if (b->h_scal.p) cudaFreeHost(b->h_scal.p);
-    if (b->h_off.p) cudaFreeHost(b->h_off.p);
-    if (b->h_out.p) cudaFreeHost(b->h_out.p);
+    b->work.release();
+    b->points.release();
+    b->table.release();
+    b->tmp.release();
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
 }
@@ -496,7 +532,8 @@ int catmsm_basis_msm_batch(void* handle, blst_p1* out, size_t nmsm, const size_t
     if (!b || !out || !counts || (!scalars && nmsm) || nmsm == 0 || nmsm > (1u << 20)) return (int)cudaErrorInvalidValue;
     int dev = -1;
     if (cudaGetDevice(&dev) != cudaSuccess || dev != b->device) return (int)cudaErrorInvalidDevice;
-    return (int)run_batch(b, out, (uint32_t)nmsm, counts, scalars, use_graph != 0);
+    std::lock_guard<std::mutex> lk(b->mu);
+    return (int)run_batch(b, &b->work, b->stream, out, (uint32_t)nmsm, counts, scalars, use_graph != 0, false);
 }
 
 int catmsm_basis_autotune(void* handle, size_t nmsm, const size_t* counts, const blst_byte* scalars, int force)
@@ -519,11 +556,15 @@ int catmsm_basis_autotune(void* handle, size_t nmsm, const size_t* counts, const
     for (uint32_t cc : cs) {
         for (uint32_t ll : ls) {
             if (catmsm_basis_set_config(b, cc, ll) != 0) continue;
-            if (run_batch(b, out.data(), (uint32_t)nmsm, counts, scalars, true) != cudaSuccess) continue;
+            if (run_batch(b, &b->work, b->stream, out.data(), (uint32_t)nmsm, counts, scalars, true, false) !=
+                cudaSuccess)
+                continue;
             float tot = 0.f;
             for (int r = 0; r < 2; r++) {
                 cudaEventRecord(e0, b->stream);
-                if (run_batch(b, out.data(), (uint32_t)nmsm, counts, scalars, true) != cudaSuccess) break;
+                if (run_batch(b, &b->work, b->stream, out.data(), (uint32_t)nmsm, counts, scalars, true, false) !=
+                    cudaSuccess)
+                    break;
                 cudaEventRecord(e1, b->stream);
                 cudaEventSynchronize(e1);
                 float ms = 0.f;

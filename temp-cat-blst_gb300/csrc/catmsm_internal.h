@@ -1,10 +1,24 @@
 // Internal declarations shared by the library's translation units.
 #pragma once
 #include "common.cuh"
+#include "catmsm_gpu.h"
 
 namespace catmsm {
 
 uint32_t msm_default_window(size_t n);
+
+// Resident basis with fixed-base tables (batch.cu) and per-worker workspaces.
+struct Basis;
+struct BatchWork;
+BatchWork* batch_work_new();
+void batch_work_free(BatchWork* w);
+// nmsm MSMs over the basis prefixes counts[j] with 32-byte scalars
+// (concatenated); Jacobian results to host `out`; synchronous on stream st.
+cudaError_t batch_run(Basis* b, BatchWork* w, cudaStream_t st, blst_p1* out, uint32_t nmsm,
+                      const size_t* counts, const uint8_t* scalars);
+size_t basis_points(const Basis* b);
+uint32_t basis_window(const Basis* b);
+int basis_device(const Basis* b);
 
 cudaError_t msm_device(Ctx* ctx, const void* d_points, const uint8_t* d_scalars, uint32_t stride,
                        size_t n, uint32_t nbits, uint32_t c, uint64_t* out);

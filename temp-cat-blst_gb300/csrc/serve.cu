@@ -1,0 +1,314 @@
+// Serving engine: continuous batching of MSM and G1 FFT requests on one GPU
+// (no reference counterpart; the reference is a synchronous library).
+//
+// State kept resident in HBM: the basis and its fixed-base tables (a Basis
+// from batch.cu).  Requests arrive from any host thread:
+//   MSM  over the first k basis points with k 32-byte scalars;
+//   FFT  of n Jacobian points with a prepared domain (forward / inverse /
+//        inverse unscaled), in place.
+// W worker threads each own a CUDA stream and a workspace.  Whenever a worker
+// is free it takes the queued requests at the head of the queue as one batch
+// -- every queued MSM, or every queued FFT, up to a point cap -- so requests
+// that arrived while other batches ran join at the next batch boundary, and
+// batches of different workers overlap on the device.  Admission is by HBM
+// budget: a batch starts only while the estimated device memory of all
+// in-flight batches stays within the budget (a single request above the
+// budget runs alone).  Every request records submit/start/done times on the
+// host's steady clock.
+#include "common.cuh"
+#include "catmsm_internal.h"
+#include "catmsm_gpu.h"
+
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <mutex>
+#include <new>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+namespace catmsm {
+
+namespace {
+
+double now_ms()
+{
+    using namespace std::chrono;
+    return duration<double, std::milli>(steady_clock::now().time_since_epoch()).count();
+}
+
+struct Request {
+    int64_t id = 0;
+    int type = 0;                       // 0 MSM, 1 FFT
+    const uint8_t* scalars = nullptr;   // MSM
+    size_t k = 0;
+    blst_p1 result;
+    blst_p1* values = nullptr;          // FFT
+    size_t n = 0;
+    const blst_fr* domain = nullptr;
+    int mode = 0;
+    size_t mem = 0;                     // admission estimate, bytes
+    double t_submit = 0, t_start = 0, t_done = 0;
+    int status = 0;
+    bool done = false;
+};
+
+struct Server;
+
+struct Worker {
+    Server* s = nullptr;
+    std::thread th;
+    BatchWork* work = nullptr;
+};
+
+struct Server {
+    Basis* basis = nullptr;
+    int device = 0;
+    size_t budget = 0, inflight = 0;
+    size_t msm_cap = 0, fft_cap = 0;    // points per batch
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::deque<Request*> queue;
+    std::unordered_map<int64_t, Request*> reqs;
+    int64_t next_id = 1;
+    bool stop = false;
+    std::vector<Worker*> workers;
+    // stats
+    long batches = 0, batched_reqs = 0, max_batch = 0;
+};
+
+size_t msm_mem(const Basis* b, size_t k)
+{
+    const size_t D = 256 / basis_window(b) + 1;
+    return k * D * 24 + ((size_t)1 << (basis_window(b) - 1)) * 192 * 2 + k * 32 + (1 << 20);
+}
+
+size_t fft_mem(size_t n) { return n * 144 * 2 + n * 64 + (1 << 20); }
+
+void worker_main(Worker* wk)
+{
+    Server* s = wk->s;
+    cudaSetDevice(s->device);
+    Ctx* ctx = get_ctx();
+    for (;;) {
+        std::vector<Request*> batch;
+        size_t mem = 0;
+        {
+            std::unique_lock<std::mutex> lk(s->mu);
+            for (;;) {
+                if (s->stop && s->queue.empty()) return;
+                if (!s->queue.empty()) {
+                    Request* h = s->queue.front();
+                    const bool fits = s->inflight + h->mem <= s->budget || s->inflight == 0;
+                    if (fits) break;
+                }
+                s->cv_work.wait(lk);
+            }
+            const int type = s->queue.front()->type;
+            size_t pts = 0;
+            for (auto it = s->queue.begin(); it != s->queue.end();) {
+                Request* r = *it;
+                const size_t rp = type == 0 ? r->k : r->n;
+                if (r->type != type) {
+                    ++it;
+                    continue;
+                }
+                const bool first = batch.empty();
+                if (!first && (pts + rp > (type == 0 ? s->msm_cap : s->fft_cap) ||
+                               s->inflight + mem + r->mem > s->budget))
+                    break;
+                batch.push_back(r);
+                pts += rp;
+                mem += r->mem;
+                it = s->queue.erase(it);
+            }
+            s->inflight += mem;
+            s->batches++;
+            s->batched_reqs += (long)batch.size();
+            s->max_batch = std::max<long>(s->max_batch, (long)batch.size());
+        }
+        const double t0 = now_ms();
+        for (Request* r : batch) r->t_start = t0;
+        int rc = 0;
+        if (!ctx) {
+            rc = (int)cudaErrorInitializationError;
+        } else if (batch[0]->type == 0) {
+            std::vector<size_t> counts(batch.size());
+            size_t total = 0;
+            for (size_t j = 0; j < batch.size(); j++) {
+                counts[j] = batch[j]->k;
+                total += batch[j]->k;
+            }
+            std::vector<uint8_t> sc(total * 32 + 32);
+            size_t off = 0;
+            for (Request* r : batch) {
+                std::memcpy(sc.data() + off, r->scalars, r->k * 32);
+                off += r->k * 32;
+            }
+            std::vector<blst_p1> out(batch.size());
+            rc = (int)batch_run(s->basis, wk->work, ctx->stream, out.data(), (uint32_t)batch.size(), counts.data(),
+                                sc.data());
+            for (size_t j = 0; j < batch.size(); j++) batch[j]->result = out[j];
+        } else {
+            std::vector<blst_p1*> vals;
+            std::vector<size_t> ns;
+            std::vector<const blst_fr*> doms;
+            std::vector<int> modes;
+            for (Request* r : batch) {
+                vals.push_back(r->values);
+                ns.push_back(r->n);
+                doms.push_back(r->domain);
+                modes.push_back(r->mode);
+            }
+            rc = catmsm_p1_fft_batch(vals.data(), ns.data(), doms.data(), modes.data(), batch.size());
+        }
+        const double t1 = now_ms();
+        {
+            std::lock_guard<std::mutex> lk(s->mu);
+            s->inflight -= mem;
+            for (Request* r : batch) {
+                r->status = rc;
+                r->t_done = t1;
+                r->done = true;
+            }
+        }
+        s->cv_done.notify_all();
+        s->cv_work.notify_all();
+    }
+}
+
+int64_t submit(Server* s, Request* r)
+{
+    r->t_submit = now_ms();
+    int64_t id;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        id = s->next_id++;
+        r->id = id;
+        s->reqs[id] = r;
+        s->queue.push_back(r);
+    }
+    s->cv_work.notify_one();
+    return id;
+}
+
+}  // namespace
+}  // namespace catmsm
+
+using namespace catmsm;
+
+extern "C" {
+
+void* catmsm_server_create(void* basis, size_t workers, size_t hbm_budget_bytes)
+{
+    if (!basis || workers == 0 || workers > 64) return nullptr;
+    Server* s = new (std::nothrow) Server();
+    if (!s) return nullptr;
+    s->basis = (Basis*)basis;
+    s->device = basis_device(s->basis);
+    s->budget = hbm_budget_bytes ? hbm_budget_bytes : ((size_t)64 << 30);
+    s->msm_cap = std::max<size_t>(basis_points(s->basis), (size_t)1 << 22);
+    s->fft_cap = (size_t)1 << 20;
+    for (size_t i = 0; i < workers; i++) {
+        Worker* w = new (std::nothrow) Worker();
+        if (!w) break;
+        w->s = s;
+        w->work = batch_work_new();
+        if (!w->work) {
+            delete w;
+            break;
+        }
+        s->workers.push_back(w);
+    }
+    if (s->workers.empty()) {
+        delete s;
+        return nullptr;
+    }
+    for (Worker* w : s->workers) w->th = std::thread(worker_main, w);
+    return s;
+}
+
+void catmsm_server_destroy(void* server)
+{
+    Server* s = (Server*)server;
+    if (!s) return;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->stop = true;
+    }
+    s->cv_work.notify_all();
+    for (Worker* w : s->workers) {
+        if (w->th.joinable()) w->th.join();
+        batch_work_free(w->work);
+        delete w;
+    }
+    for (auto& kv : s->reqs) delete kv.second;
+    delete s;
+}
+
+int64_t catmsm_server_submit_msm(void* server, const blst_byte* scalars, size_t k)
+{
+    Server* s = (Server*)server;
+    if (!s || !scalars || k == 0 || k > basis_points(s->basis)) return -1;
+    Request* r = new (std::nothrow) Request();
+    if (!r) return -1;
+    r->type = 0;
+    r->scalars = scalars;
+    r->k = k;
+    r->mem = msm_mem(s->basis, k);
+    return submit(s, r);
+}
+
+int64_t catmsm_server_submit_fft(void* server, blst_p1* values, size_t n, const blst_fr* domain, int mode)
+{
+    Server* s = (Server*)server;
+    if (!s || !values || !domain || n == 0 || (n & (n - 1)) || mode < 0 || mode > 2) return -1;
+    Request* r = new (std::nothrow) Request();
+    if (!r) return -1;
+    r->type = 1;
+    r->values = values;
+    r->n = n;
+    r->domain = domain;
+    r->mode = mode;
+    r->mem = fft_mem(n);
+    return submit(s, r);
+}
+
+int catmsm_server_wait(void* server, int64_t ticket, blst_p1* msm_out, double* times_ms)
+{
+    Server* s = (Server*)server;
+    if (!s) return (int)cudaErrorInvalidValue;
+    Request* r = nullptr;
+    {
+        std::unique_lock<std::mutex> lk(s->mu);
+        auto it = s->reqs.find(ticket);
+        if (it == s->reqs.end()) return (int)cudaErrorInvalidValue;
+        r = it->second;
+        s->cv_done.wait(lk, [&] { return r->done; });
+        s->reqs.erase(it);
+    }
+    if (msm_out && r->type == 0) *msm_out = r->result;
+    if (times_ms) {
+        times_ms[0] = r->t_start - r->t_submit;   // queueing
+        times_ms[1] = r->t_done - r->t_submit;    // latency
+    }
+    const int rc = r->status;
+    delete r;
+    return rc;
+}
+
+int catmsm_server_stats(void* server, long* batches, long* batched_requests, long* max_batch)
+{
+    Server* s = (Server*)server;
+    if (!s) return (int)cudaErrorInvalidValue;
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (batches) *batches = s->batches;
+    if (batched_requests) *batched_requests = s->batched_reqs;
+    if (max_batch) *max_batch = s->max_batch;
+    return 0;
+}
+
+}  // extern "C"
