@@ -280,6 +280,196 @@ def batched_section(g, synth, torch, dev, steps, warmup, peak):
                       "launch, D2H of results)"}
 
 
+def fft_canonical_m(n, inverse=False):
+    """Canonical Montgomery-multiplication count of the reference G1 FFT."""
+    lg = n.bit_length() - 1
+    m = ((n // 2) * lg - (n - 1)) * 1976 + (n // 2) * lg * 36
+    return m + (n * 1976 if inverse else 0)
+
+
+def _jacobian_z1(aff: bytes, n: int) -> bytes:
+    one = ((1 << 384) % P_MOD).to_bytes(48, "little")
+    return b"".join(aff[96 * i:96 * i + 96] + one for i in range(n))
+
+
+def batched_fft_section(g, synth, torch, dev, steps, warmup, peak):
+    """BASELINE config 4: 64 transforms per batch, 16 each of 2^10, 2^12, 2^14,
+    2^16 in a seeded order, seeded points in Jacobian form, prepared domains;
+    forward and inverse batches through catmsm_p1_fft_batch (host buffers, one
+    launch per stage level for all transforms) vs the same 64 transforms as
+    plain per-call blst_p1_fft_with_domain."""
+    import numpy as np
+    rng = np.random.default_rng(4)
+    sizes = [1 << e for e in (10, 12, 14, 16) for _ in range(16)]
+    rng.shuffle(sizes)
+    sizes = [int(x) for x in sizes]
+    biggest = max(sizes)
+    k_pts = torch.frombuffer(bytearray(synth.point_scalars(4, biggest)), dtype=torch.uint8).to(dev)
+    d_pts = torch.empty(biggest * 96, dtype=torch.uint8, device=dev)
+    torch.cuda.synchronize()
+    assert g.load().catmsm_p1_affines_from_scalars_device(d_pts.data_ptr(), k_pts.data_ptr(), biggest) == 0
+    aff = bytes(d_pts.cpu().numpy())
+    base = {n: _jacobian_z1(aff, n) for n in sorted(set(sizes))}
+    doms = {n: g.fr_fft_domain_init(n)[1] for n in base}
+    vals = [base[n] for n in sizes]
+    res = {}
+    for mode, name in ((0, "forward"), (1, "inverse")):
+        for _ in range(max(1, warmup // 2)):
+            rc, outs = g.p1_fft_batch(vals, sizes, [doms[n] for n in sizes], [mode] * len(sizes))
+            assert rc == 0
+        ts = []
+        for _ in range(max(1, steps // 3)):
+            t = time.perf_counter()
+            rc, outs = g.p1_fft_batch(vals, sizes, [doms[n] for n in sizes], [mode] * len(sizes))
+            ts.append(time.perf_counter() - t)
+            assert rc == 0
+        tb = statistics.mean(ts)
+        cm = sum(fft_canonical_m(n, mode == 1) for n in sizes)
+        res[name] = {"transforms_per_s": len(sizes) / tb, "ms_per_batch": tb * 1e3,
+                     "canonical_timad_s": cm * IMAD_PER_M / tb / 1e12,
+                     "canonical_frac_of_peak": cm * IMAD_PER_M / tb / 1e12 / peak if peak > 0 else None}
+        if mode == 0:
+            fwd = outs
+    # round trip on one transform of each size, and parity with the per-call path
+    rt, par = True, True
+    for n in sorted(base):
+        i = sizes.index(n)
+        ok, back = g.p1_fft_with_domain(fwd[i], n, doms[n], n + 2, True)
+        ok2, single = g.p1_fft_with_domain(vals[i], n, doms[n], n + 2, False)
+        for j in range(0, n, max(1, n // 64)):
+            rt &= _jac_affine(back[144 * j:144 * j + 144]) == _jac_affine(vals[i][144 * j:144 * j + 144])
+            par &= _jac_affine(single[144 * j:144 * j + 144]) == _jac_affine(fwd[i][144 * j:144 * j + 144])
+    # plain per-call path, forward
+    t = time.perf_counter()
+    for n, v in zip(sizes, vals):
+        ok, _ = g.p1_fft_with_domain(v, n, doms[n], n + 2, False)
+        assert ok
+    t_plain = time.perf_counter() - t
+    res["plain_forward_transforms_per_s"] = len(sizes) / t_plain
+    res["speedup_vs_plain_forward"] = t_plain / (res["forward"]["ms_per_batch"] * 1e-3)
+    res["round_trip_ok"] = rt
+    res["parity_vs_per_call_path"] = par
+    res["workload"] = ("64 transforms/batch: 16 each of 2^10, 2^12, 2^14, 2^16 (seeded order), Jacobian "
+                       "inputs (z = 1), prepared domains; host buffers, H2D/D2H inside the timer")
+    return res
+
+
+def serving_section(g, synth, torch, dev, rates, seconds):
+    """BASELINE config 5: Poisson arrivals (swept rate) of 70% MSMs with k
+    log-uniform in [2^10, 2^22] over a resident 2^22-point basis (fixed-base
+    tables) and 30% G1 FFTs with n = 2^(12..16); served by the continuous-
+    batching engine vs a plain FIFO server making one per-call request at a
+    time.  Latency = submit to completion (host steady clock)."""
+    import numpy as np
+    import threading
+    nb = 1 << 22
+    k_pts = torch.frombuffer(bytearray(synth.point_scalars(5, nb)), dtype=torch.uint8).to(dev)
+    d_pts = torch.empty(nb * 96, dtype=torch.uint8, device=dev)
+    torch.cuda.synchronize()
+    assert g.load().catmsm_p1_affines_from_scalars_device(d_pts.data_ptr(), k_pts.data_ptr(), nb) == 0
+    del k_pts
+    pts = bytes(d_pts.cpu().numpy())
+    import ctypes
+    pool = bytearray(synth.scalars(5005, nb, 0))        # scalars of a request: a slice of the pool
+    pool_addr = ctypes.addressof((ctypes.c_char * len(pool)).from_buffer(pool))
+    d_pool = torch.frombuffer(pool, dtype=torch.uint8).to(dev)
+    fsizes = [1 << e for e in range(12, 17)]
+    fjac = {n: _jacobian_z1(pts, n) for n in fsizes}
+    fdom = {n: g.fr_fft_domain_init(n)[1] for n in fsizes}
+    t0 = time.perf_counter()
+    basis = g.Basis(pts, nb, 13)
+    build_s = time.perf_counter() - t0
+    out = {"workload": "Poisson arrivals; 70%% MSM, k = floor(2^U), U ~ U[10, 22], over a resident 2^22-point "
+                       "basis with fixed-base tables (c = 13); 30%% G1 FFT, n = 2^(12..16) uniform; "
+                       "%.0f s per rate" % seconds, "basis_table_build_s": build_s, "rates": []}
+    for rate in rates:
+        rng = np.random.default_rng(int(rate * 1000))
+        arrivals, reqs, t = [], [], 0.0
+        while True:
+            t += rng.exponential(1.0 / rate)
+            if t > seconds:
+                break
+            arrivals.append(t)
+            if rng.random() < 0.7:
+                k = int(2 ** rng.uniform(10, 22))
+                off = int(rng.integers(0, nb - k + 1))
+                reqs.append(("msm", k, off))
+            else:
+                reqs.append(("fft", int(fsizes[rng.integers(0, len(fsizes))])))
+        row = {"rate_per_s": rate, "requests": len(reqs)}
+        for mode in ("engine", "plain"):
+            lat = [0.0] * len(reqs)
+            server = g.Server(basis, workers=4, hbm_budget=48 << 30) if mode == "engine" else None
+            done = threading.Event()
+            q = []
+            cv = threading.Condition()
+            start = time.perf_counter()
+
+            def producer():
+                for i, (a, r) in enumerate(zip(arrivals, reqs)):
+                    dt = start + a - time.perf_counter()
+                    if dt > 0:
+                        time.sleep(dt)
+                    ts = time.perf_counter()
+                    if mode == "engine":
+                        if r[0] == "msm":
+                            tk = server.submit_msm_ptr(pool_addr + 32 * r[2], r[1])
+                        else:
+                            tk = server.submit_fft(fjac[r[1]], r[1], fdom[r[1]], 0)
+                        with cv:
+                            q.append((i, ts, tk))
+                            cv.notify()
+                    else:
+                        with cv:
+                            q.append((i, ts, None))
+                            cv.notify()
+                with cv:
+                    q.append(None)
+                    cv.notify()
+
+            def consumer():
+                while True:
+                    with cv:
+                        while not q:
+                            cv.wait()
+                        item = q.pop(0)
+                    if item is None:
+                        return
+                    i, ts, tk = item
+                    r = reqs[i]
+                    if mode == "engine":
+                        rc, _, _, lat_ms = server.wait(tk)
+                        assert rc == 0
+                        lat[i] = lat_ms                   # submit -> done, measured by the engine
+                        continue
+                    if r[0] == "msm":
+                        g.msm_device(d_pts.data_ptr(), d_pool.data_ptr() + 32 * r[2], 32, r[1], 256)
+                    else:
+                        ok, _ = g.p1_fft_with_domain(fjac[r[1]], r[1], fdom[r[1]], r[1] + 2, False)
+                        assert ok
+                    lat[i] = (time.perf_counter() - ts) * 1e3
+
+            pt = threading.Thread(target=producer)
+            ct = threading.Thread(target=consumer)
+            pt.start()
+            ct.start()
+            pt.join()
+            ct.join()
+            wall = time.perf_counter() - start
+            st = server.stats() if server else None
+            if server:
+                server.close()
+            lat_sorted = sorted(lat)
+            row[mode] = {"throughput_req_per_s": len(reqs) / wall,
+                         "p50_ms": lat_sorted[len(lat) // 2] if lat else None,
+                         "p99_ms": lat_sorted[min(len(lat) - 1, int(0.99 * len(lat)))] if lat else None,
+                         "mean_batch": (st["requests"] / st["batches"]) if st and st["batches"] else 1.0}
+        out["rates"].append(row)
+        print("serving rate %.1f/s done" % rate, file=sys.stderr, flush=True)
+    basis.close()
+    return out
+
+
 def run_ours(args, ws, rank, local):
     import torch
     torch.cuda.set_device(local)
@@ -404,9 +594,13 @@ def run_ours(args, ws, rank, local):
                "sample": "%d whole single-window tiles (c=%d, of D=%d) of the same 2^%d-point MSM, "
                          "1 thread, %.1f s; the reference's Pippenger restated in C (oracle/)"
                          % (tiles, cref, 1 + NBITS // cref, n.bit_length() - 1, el)}
-    batched = None
-    if not args.no_batched:
+    batched = fft_batch = serving = None
+    if ws == 1 and not args.no_batched:
         batched = batched_section(g, synth, torch, dev, args.steps, args.warmup, peak)
+        fft_batch = batched_fft_section(g, synth, torch, dev, args.steps, args.warmup, peak)
+    if ws == 1 and not args.no_serving:
+        serving = serving_section(g, synth, torch, dev, [float(r) for r in args.serve_rates.split(",")],
+                                  args.serve_seconds)
     line = {
         "metric": METRIC, "value": ws * n / (t_mean * 1e-3) / 1e6, "unit": UNIT, "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_mean, "higher_is_better": True,
@@ -432,6 +626,8 @@ def run_ours(args, ws, rank, local):
         "cpu_baseline": cpu,
         "clocks": clk,
         "batched_commitments": batched,
+        "batched_fft": fft_batch,
+        "serving": serving,
     }
     print(json.dumps(line))
     if dist is not None:
@@ -470,7 +666,10 @@ def main():
     ap.add_argument("--n", type=int, default=N_POINTS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--window", type=int, default=0, help="MSM window width (0 = library default)")
-    ap.add_argument("--no-batched", action="store_true", help="skip the batched-commitments section")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched MSM / FFT sections")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving sweep")
+    ap.add_argument("--serve-rates", default="25,50,100,150", help="Poisson arrival rates (requests/s)")
+    ap.add_argument("--serve-seconds", type=float, default=3.0, help="arrival window per rate")
     args = ap.parse_args()
     ws, rank, local = dist_setup()
     if args.impl == "reference":

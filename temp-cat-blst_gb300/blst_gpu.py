@@ -375,6 +375,15 @@ class Server:
         self._keep[t] = (buf,)
         return t
 
+    def submit_msm_ptr(self, addr: int, k: int) -> int:
+        """MSM request whose k scalars live at host address `addr` (no copy;
+        the caller keeps that memory alive until wait returns)."""
+        t = self.L.catmsm_server_submit_msm(self.h, addr, k)
+        if t < 0:
+            raise ValueError("submit_msm rejected")
+        self._keep[t] = ()
+        return t
+
     def submit_fft(self, values: bytes, n: int, domain: bytes, mode: int) -> int:
         vb = (C.c_char * len(values)).from_buffer_copy(values)
         db = (C.c_char * len(domain)).from_buffer_copy(domain)
