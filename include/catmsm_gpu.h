@@ -90,6 +90,29 @@ bool blst_p1_fft_with_domain(blst_p1 *values, size_t n, const blst_fr *domain, s
  * blst/fft_c_api.cpp:208): the inverse transform without the 1/n scale. */
 bool blst_p1_ifft_unscaled_with_domain(blst_p1 *values, size_t n, const blst_fr *domain, size_t domain_len);
 
+/* Replaces blst_p1s_mult_pippenger_fr_scratch_sizeof (bindings/blst_scalar.h:541,
+ * blst/c_api.cpp:1420 -> :271-296): n*32 scalar bytes plus 192 * 2^(c(n)-1)
+ * bucket bytes for n > 1; 0 for n == 0 or an unrepresentable size. */
+size_t blst_p1s_mult_pippenger_fr_scratch_sizeof(size_t npoints);
+
+/* Replaces blst_p1s_mult_pippenger_fr (bindings/blst_scalar.h:549,
+ * blst/c_api.cpp:1425-1435 -> :532-585): MSM of contiguous points with
+ * Montgomery-form blst_fr scalars (converted to canonical integers, 255 bits).
+ * NULL ret -> false; n == 0 -> infinity and true; NULL points/scalars/scratch
+ * or scratch_size below the queried size -> false with ret unchanged. */
+bool blst_p1s_mult_pippenger_fr(blst_p1 *ret, const blst_p1_affine points[], const blst_fr scalars[],
+                                size_t npoints, blst_limb_t *scratch, size_t scratch_size);
+
+/* Replaces blst_fr_fft (bindings/blst_fft.h:41, blst/fft_c_api.cpp:109-126):
+ * in-place Fr DFT with powers of the primitive n-th root (inverse: of its
+ * reciprocal, scaled by 1/n); false before writing on NULL or invalid n. */
+bool blst_fr_fft(blst_fr *values, size_t n, bool inverse);
+
+/* Replaces blst_fr_fft_with_domain (bindings/blst_fft.h:87, blst/fft_c_api.cpp:
+ * 150-182): prepared-domain Fr DFT; the inverse reads forward roots at n - idx
+ * and scales by domain[n]; false before writing on a bad length or tag. */
+bool blst_fr_fft_with_domain(blst_fr *values, size_t n, const blst_fr *domain, size_t domain_len, bool inverse);
+
 /* ------------------------------------------------------------------ Part 2 */
 
 /* MSM over DEVICE-resident inputs (no reference counterpart): d_points is n

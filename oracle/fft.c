@@ -180,13 +180,9 @@ bool oracle_p1_ifft_unscaled_with_domain(op1 *values, size_t n, const ofr *domai
     return true;
 }
 
-/* ---- Fr FFT (fft_c_api.cpp:109-126), used for FFT-in-the-exponent checks ---- */
-bool oracle_fr_fft(ofr *a, size_t n, bool inverse)
+/* ---- Fr FFT (fft_c_api.cpp:109-182; FrCoeffCtx context.h:25-64) ---- */
+static void fr_butterflies(ofr *a, size_t n, const ofr *roots, int inverse_from_forward)
 {
-    if (!a || !valid_size(n)) return false;
-    ofr *roots = (ofr *)malloc(n * sizeof(ofr));
-    if (!roots) return false;
-    fill_roots(roots, n, inverse);
     for (size_t i = 1, j = 0; i < n; i++) {
         size_t bit = n >> 1;
         for (; j & bit; bit >>= 1) j ^= bit;
@@ -199,7 +195,10 @@ bool oracle_fr_fft(ofr *a, size_t n, bool inverse)
         for (size_t i = 0; i < n; i += len) {
             for (size_t j = 0; j < half; j++) {
                 ofr u = a[i + j], t;
-                ofr_mul(&t, &a[i + j + half], &roots[j * (n / len)]);
+                size_t idx = j * (n / len);
+                if (inverse_from_forward && j) idx = n - idx;
+                if (j) ofr_mul(&t, &a[i + j + half], &roots[idx]);
+                else t = a[i + j + half];
                 /* u + t, u - t mod r */
                 unsigned __int128 c = 0;
                 ofr s, d;
@@ -215,6 +214,15 @@ bool oracle_fr_fft(ofr *a, size_t n, bool inverse)
             }
         }
     }
+}
+
+bool oracle_fr_fft(ofr *a, size_t n, bool inverse)
+{
+    if (!a || !valid_size(n)) return false;
+    ofr *roots = (ofr *)malloc(n * sizeof(ofr));
+    if (!roots) return false;
+    fill_roots(roots, n, inverse);
+    fr_butterflies(a, n, roots, 0);
     if (inverse) {
         ofr nn, inv;
         ofr_from_u64(&nn, n);
@@ -222,5 +230,14 @@ bool oracle_fr_fft(ofr *a, size_t n, bool inverse)
         for (size_t i = 0; i < n; i++) ofr_mul(&a[i], &a[i], &inv);
     }
     free(roots);
+    return true;
+}
+
+bool oracle_fr_fft_with_domain(ofr *a, size_t n, const ofr *domain, size_t domain_len, bool inverse)
+{
+    if (!a || !domain_ok(n, domain, domain_len)) return false;
+    fr_butterflies(a, n, domain, inverse ? 1 : 0);
+    if (inverse)
+        for (size_t i = 0; i < n; i++) ofr_mul(&a[i], &a[i], &domain[n]);
     return true;
 }

@@ -100,6 +100,7 @@ bool oracle_p1_fft(op1 *values, size_t n, bool inverse);
 bool oracle_p1_fft_with_domain(op1 *values, size_t n, const ofr *domain, size_t domain_len, bool inverse);
 bool oracle_p1_ifft_unscaled_with_domain(op1 *values, size_t n, const ofr *domain, size_t domain_len);
 bool oracle_fr_fft(ofr *values, size_t n, bool inverse);
+bool oracle_fr_fft_with_domain(ofr *values, size_t n, const ofr *domain, size_t domain_len, bool inverse);
 void oracle_fr_root_of_unity(ofr *o, size_t log2n);
 
 /* ---- seeded synthetic inputs (gen.c) ---- */

@@ -100,6 +100,8 @@ class Oracle(_Common):
         L.oracle_p1_ifft_unscaled_with_domain.argtypes = [_vp, _sz, _vp, _sz]
         L.oracle_fr_fft.restype = C.c_bool
         L.oracle_fr_fft.argtypes = [_vp, _sz, C.c_bool]
+        L.oracle_fr_fft_with_domain.restype = C.c_bool
+        L.oracle_fr_fft_with_domain.argtypes = [_vp, _sz, _vp, _sz, C.c_bool]
         L.oracle_gen_scalars.argtypes = [C.c_uint64, _sz, C.c_int, _vp]
         L.oracle_points_from_scalars.argtypes = [_vp, _sz, _vp, C.c_int]
         L.oracle_duplicate_points.argtypes = [C.c_uint64, _sz, _vp]
@@ -232,6 +234,16 @@ class Oracle(_Common):
         ok = self.L.oracle_fr_fft(_buf(b), n, inverse)
         return ok, bytes(b)
 
+    def fr_fft_with_domain(self, values, n, domain, domain_len, inverse):
+        b = bytearray(values)
+        ok = self.L.oracle_fr_fft_with_domain(_buf(b), n, _buf(domain), domain_len, inverse)
+        return ok, bytes(b)
+
+    def msm_fr(self, points: bytes, frs: bytes, n: int) -> bytes:
+        """blst_p1s_mult_pippenger_fr semantics: Montgomery Fr scalars."""
+        canon = b"".join(self.fr_from_mont(frs[32 * i:32 * i + 32]) for i in range(n))
+        return self.msm(points, canon, n, 255)
+
     def fr_to_mont(self, canon: bytes) -> bytes:
         out = bytearray(32)
         self.L.ofr_to_mont(_buf(out), _buf(canon))
@@ -273,6 +285,12 @@ class Reference(_Common):
         L.blst_p1_ifft_unscaled_with_domain.argtypes = [_vp, _sz, _vp, _sz]
         L.blst_fr_fft.restype = C.c_bool
         L.blst_fr_fft.argtypes = [_vp, _sz, C.c_bool]
+        L.blst_fr_fft_with_domain.restype = C.c_bool
+        L.blst_fr_fft_with_domain.argtypes = [_vp, _sz, _vp, _sz, C.c_bool]
+        L.blst_p1s_mult_pippenger_fr_scratch_sizeof.restype = _sz
+        L.blst_p1s_mult_pippenger_fr_scratch_sizeof.argtypes = [_sz]
+        L.blst_p1s_mult_pippenger_fr.restype = C.c_bool
+        L.blst_p1s_mult_pippenger_fr.argtypes = [_vp, _vp, _vp, _sz, _vp, _sz]
         self._msm = L.blst_p1s_mult_pippenger
         self.scratch_sizeof = L.blst_p1s_mult_pippenger_scratch_sizeof
 
@@ -333,6 +351,19 @@ class Reference(_Common):
         b = bytearray(values)
         ok = self.L.blst_fr_fft(_buf(b), n, inverse)
         return ok, bytes(b)
+
+    def fr_fft_with_domain(self, values, n, domain, domain_len, inverse):
+        b = bytearray(values)
+        ok = self.L.blst_fr_fft_with_domain(_buf(b), n, _buf(domain), domain_len, inverse)
+        return ok, bytes(b)
+
+    def msm_fr(self, points: bytes, frs: bytes, n: int) -> bytes:
+        sz = self.L.blst_p1s_mult_pippenger_fr_scratch_sizeof(n)
+        scratch = (C.c_uint64 * (sz // 8 + 1))()
+        ret = bytearray(P1)
+        ok = self.L.blst_p1s_mult_pippenger_fr(_buf(ret), _buf(points), _buf(frs), n, scratch, sz)
+        assert ok
+        return self.compress(bytes(ret))
 
 
 def reference_available():

@@ -62,6 +62,14 @@ def load(build_if_missing=True):
     L.catmsm_p1s_mult_pippenger_device.argtypes = [_vp, _vp, _vp, _sz, _sz, _sz, _sz]
     L.catmsm_p1_fft_device.restype = C.c_int
     L.catmsm_p1_fft_device.argtypes = [_vp, _sz, _vp, C.c_int]
+    L.blst_p1s_mult_pippenger_fr_scratch_sizeof.restype = _sz
+    L.blst_p1s_mult_pippenger_fr_scratch_sizeof.argtypes = [_sz]
+    L.blst_p1s_mult_pippenger_fr.restype = C.c_bool
+    L.blst_p1s_mult_pippenger_fr.argtypes = [_vp, _vp, _vp, _sz, _vp, _sz]
+    L.blst_fr_fft.restype = C.c_bool
+    L.blst_fr_fft.argtypes = [_vp, _sz, C.c_bool]
+    L.blst_fr_fft_with_domain.restype = C.c_bool
+    L.blst_fr_fft_with_domain.argtypes = [_vp, _sz, _vp, _sz, C.c_bool]
     L.catmsm_p1_fft_batch.restype = C.c_int
     L.catmsm_p1_fft_batch.argtypes = [_vp, _vp, _vp, _vp, _sz]
     L.catmsm_stream.restype = _vp
@@ -191,6 +199,35 @@ def p1_ifft_unscaled_with_domain(values: bytes, n: int, domain: bytes, domain_le
     b = bytearray(values)
     ok = load().blst_p1_ifft_unscaled_with_domain(_buf(b) if b else None, n, _buf(domain) if domain else None,
                                                   domain_len)
+    return ok, bytes(b)
+
+
+def p1s_mult_pippenger_fr(points: bytes, frs: bytes, n: int, scratch_size=None, ret_init=None):
+    """blst_p1s_mult_pippenger_fr; returns (ok, 144-byte ret)."""
+    L = load()
+    need = L.blst_p1s_mult_pippenger_fr_scratch_sizeof(n)
+    size = need if scratch_size is None else scratch_size
+    scratch = (C.c_uint64 * (max(size, 8) // 8 + 1))() if size >= 0 else None
+    ret = bytearray(ret_init if ret_init is not None else bytes(P1))
+    ok = L.blst_p1s_mult_pippenger_fr(_buf(ret), _buf(bytearray(points)) if points else None,
+                                      _buf(bytearray(frs)) if frs else None, n, scratch, size if size >= 0 else 0)
+    return ok, bytes(ret)
+
+
+def p1s_mult_pippenger_fr_scratch_sizeof(n: int) -> int:
+    return load().blst_p1s_mult_pippenger_fr_scratch_sizeof(n)
+
+
+def fr_fft(values: bytes, n: int, inverse: bool):
+    b = bytearray(values)
+    ok = load().blst_fr_fft(_buf(b) if b else None, n, inverse)
+    return ok, bytes(b)
+
+
+def fr_fft_with_domain(values: bytes, n: int, domain: bytes, domain_len: int, inverse: bool):
+    b = bytearray(values)
+    ok = load().blst_fr_fft_with_domain(_buf(b) if b else None, n, _buf(domain) if domain else None,
+                                        domain_len, inverse)
     return ok, bytes(b)
 
 

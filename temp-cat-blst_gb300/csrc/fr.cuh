@@ -64,6 +64,40 @@ __device__ __forceinline__ void fr_mul(uint32_t* o, const uint32_t* a, const uin
     for (int i = 0; i < 8; i++) o[i] = t[i];
 }
 
+// o = a + b mod r, o = a - b mod r (reduced inputs and outputs)
+__device__ __forceinline__ void fr_add(uint32_t* o, const uint32_t* a, const uint32_t* b)
+{
+    uint32_t t[8];
+    uint64_t c = 0;
+    for (int i = 0; i < 8; i++) {
+        c += (uint64_t)a[i] + b[i];
+        t[i] = (uint32_t)c;
+        c >>= 32;
+    }
+    if (c || fr_geq(t, FR_R)) fr_sub_r(t);
+    for (int i = 0; i < 8; i++) o[i] = t[i];
+}
+
+__device__ __forceinline__ void fr_sub(uint32_t* o, const uint32_t* a, const uint32_t* b)
+{
+    uint32_t t[8];
+    uint64_t br = 0;
+    for (int i = 0; i < 8; i++) {
+        const uint64_t d = (uint64_t)a[i] - b[i] - br;
+        t[i] = (uint32_t)d;
+        br = (d >> 63) & 1;
+    }
+    if (br) {
+        uint64_t c = 0;
+        for (int i = 0; i < 8; i++) {
+            c += (uint64_t)t[i] + FR_R[i];
+            t[i] = (uint32_t)c;
+            c >>= 32;
+        }
+    }
+    for (int i = 0; i < 8; i++) o[i] = t[i];
+}
+
 __device__ __forceinline__ void fr_from_mont(uint32_t* o, const uint32_t* a)
 {
     const uint32_t one[8] = {1, 0, 0, 0, 0, 0, 0, 0};

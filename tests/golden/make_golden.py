@@ -10,6 +10,8 @@ reference's own C ABI built from its sources (oracle/_ref/libblst_ref.so):
           -> blst_p1_serialize of every element; small n stored in full,
           larger n as sha256 of the concatenation
   * domain: blst_fr_fft_domain_init bytes (sha256) per size
+  * msm_fr: blst_p1s_mult_pippenger_fr (Montgomery Fr scalars) -> compressed
+  * fr_fft: blst_fr_fft / blst_fr_fft_with_domain output bytes (sha256)
 """
 import hashlib
 import json
@@ -90,6 +92,30 @@ def main():
                 entry["serialized"] = ser.hex()
             g["fft"].append(entry)
             print("fft", seed, n, mode, "%.1fs" % (time.time() - t), flush=True)
+    # Fr-scalar MSM (blst_p1s_mult_pippenger_fr): Montgomery Fr scalars
+    g["msm_fr"] = []
+    for seed, n in ((41, 1), (42, 2), (43, 100), (44, 4096), (45, 1 << 14)):
+        pts = o.gen_points(seed, n)
+        frs = b"".join(o.fr_to_mont(o.gen_scalars(seed + 1000, n, 0)[32 * i:32 * i + 32]) for i in range(n))
+        g["msm_fr"].append({"seed": seed, "n": n, "compressed": r.msm_fr(pts, frs, n).hex()})
+        print("msm_fr", seed, n, flush=True)
+    # Fr FFT (blst_fr_fft / blst_fr_fft_with_domain): values = seeded Fr in Montgomery form
+    g["fr_fft"] = []
+    for seed, n in ((51, 1), (52, 2), (53, 8), (54, 256), (55, 2048), (56, 4096), (57, 1 << 16)):
+        vals = b"".join(o.fr_to_mont(o.gen_scalars(seed, n, 0)[32 * i:32 * i + 32]) for i in range(n))
+        d = r.domain(n)
+        for mode in ("fwd", "inv", "dfwd", "dinv"):
+            if mode == "fwd":
+                ok, out = r.fr_fft(vals, n, False)
+            elif mode == "inv":
+                ok, out = r.fr_fft(vals, n, True)
+            elif mode == "dfwd":
+                ok, out = r.fr_fft_with_domain(vals, n, d, n + 2, False)
+            else:
+                ok, out = r.fr_fft_with_domain(vals, n, d, n + 2, True)
+            assert ok
+            g["fr_fft"].append({"seed": seed, "n": n, "mode": mode, "sha256": hashlib.sha256(out).hexdigest()})
+        print("fr_fft", seed, n, flush=True)
     if not large and os.path.exists(OUT):
         # keep previously generated large cases
         old = json.load(open(OUT))

@@ -147,3 +147,28 @@ def test_oracle_matches_reference_descriptor_arrays(oracle):
     oracle.L.oracle_p1s_mult_pippenger((C.c_char * 144).from_buffer(r1), pa, n, sa, 255, None)
     ref.L.blst_p1s_mult_pippenger((C.c_char * 144).from_buffer(r2), pa, n, sa, 255, None)
     assert oracle.compress(bytes(r1)) == ref.compress(bytes(r2)) == bytes([0xC0]) + bytes(47)
+
+
+def _frs(oracle, seed, n):
+    sc = oracle.gen_scalars(seed, n, 0)
+    return b"".join(oracle.fr_to_mont(sc[32 * i:32 * i + 32]) for i in range(n))
+
+
+def test_oracle_msm_fr_matches_golden(golden, oracle):
+    for c in golden["msm_fr"]:
+        n = c["n"]
+        pts = oracle.gen_points(c["seed"], n)
+        frs = _frs(oracle, c["seed"] + 1000, n)
+        assert oracle.msm_fr(pts, frs, n).hex() == c["compressed"], n
+
+
+def test_oracle_fr_fft_matches_golden(golden, oracle):
+    for c in golden["fr_fft"]:
+        n = c["n"]
+        vals = _frs(oracle, c["seed"], n)
+        d = oracle.domain(n)
+        if c["mode"] in ("fwd", "inv"):
+            ok, out = oracle.fr_fft(vals, n, c["mode"] == "inv")
+        else:
+            ok, out = oracle.fr_fft_with_domain(vals, n, d, n + 2, c["mode"] == "dinv")
+        assert ok and hashlib.sha256(out).hexdigest() == c["sha256"], (n, c["mode"])
