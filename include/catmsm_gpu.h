@@ -242,6 +242,22 @@ int64_t catmsm_server_submit_fft(void *server, blst_p1 *values, size_t n, const 
 int catmsm_server_wait(void *server, int64_t ticket, blst_p1 *msm_out, double *times_ms);
 int catmsm_server_stats(void *server, long *batches, long *batched_requests, long *max_batch);
 
+/* ---- Batched point decoding and validation (no single reference call; each
+ * element has exactly the semantics of the reference call cited):
+ * catmsm_p1s_uncompress  = blst_p1_uncompress (bindings/blst_scalar.h:623) on
+ *                          48-byte element i of in48;
+ * catmsm_p1s_deserialize = blst_p1_deserialize (bindings/blst_scalar.h:631) on
+ *                          96-byte element i of in96;
+ * errs[i] receives the BLST_ERROR value (0 success, 1 bad encoding, 2 not on
+ * curve, 3 not in group); out[i] is written only on success.  check_group != 0
+ * adds blst_p1_affine_in_g1 to every successful decode (POINT_NOT_IN_GROUP on
+ * failure).  catmsm_p1s_affine_in_g1 = blst_p1_affine_in_g1
+ * (bindings/blst_scalar.h:507) per point: results[i] = 1 member, 0 not.
+ * Host buffers; return 0 or a cudaError_t value. */
+int catmsm_p1s_uncompress(blst_p1_affine *out, const blst_byte *in48, size_t n, int *errs, int check_group);
+int catmsm_p1s_deserialize(blst_p1_affine *out, const blst_byte *in96, size_t n, int *errs, int check_group);
+int catmsm_p1s_affine_in_g1(const blst_p1_affine *points, size_t n, int *results);
+
 /* Field self-check: out[i] = a[i] * b[i] * R^-1 mod p (canonical), host
  * buffers of n blst_fp.  Returns 0 on success. */
 int catmsm_fp_mul(blst_fp *out, const blst_fp *a, const blst_fp *b, size_t n);

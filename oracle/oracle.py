@@ -287,6 +287,12 @@ class Reference(_Common):
         L.blst_fr_fft.argtypes = [_vp, _sz, C.c_bool]
         L.blst_fr_fft_with_domain.restype = C.c_bool
         L.blst_fr_fft_with_domain.argtypes = [_vp, _sz, _vp, _sz, C.c_bool]
+        L.blst_p1_uncompress.restype = C.c_int
+        L.blst_p1_uncompress.argtypes = [_vp, _vp]
+        L.blst_p1_deserialize.restype = C.c_int
+        L.blst_p1_deserialize.argtypes = [_vp, _vp]
+        L.blst_p1_affine_in_g1.restype = C.c_bool
+        L.blst_p1_affine_in_g1.argtypes = [_vp]
         L.blst_p1s_mult_pippenger_fr_scratch_sizeof.restype = _sz
         L.blst_p1s_mult_pippenger_fr_scratch_sizeof.argtypes = [_sz]
         L.blst_p1s_mult_pippenger_fr.restype = C.c_bool
@@ -356,6 +362,19 @@ class Reference(_Common):
         b = bytearray(values)
         ok = self.L.blst_fr_fft_with_domain(_buf(b), n, _buf(domain), domain_len, inverse)
         return ok, bytes(b)
+
+    def uncompress(self, enc48: bytes, init: bytes = bytes(96)):
+        out = bytearray(init)
+        err = self.L.blst_p1_uncompress(_buf(out), _buf(enc48))
+        return err, bytes(out)
+
+    def deserialize(self, enc96: bytes, init: bytes = bytes(96)):
+        out = bytearray(init)
+        err = self.L.blst_p1_deserialize(_buf(out), _buf(enc96))
+        return err, bytes(out)
+
+    def in_g1(self, aff: bytes) -> bool:
+        return bool(self.L.blst_p1_affine_in_g1(_buf(aff)))
 
     def msm_fr(self, points: bytes, frs: bytes, n: int) -> bytes:
         sz = self.L.blst_p1s_mult_pippenger_fr_scratch_sizeof(n)

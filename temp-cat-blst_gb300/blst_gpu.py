@@ -70,6 +70,11 @@ def load(build_if_missing=True):
     L.blst_fr_fft.argtypes = [_vp, _sz, C.c_bool]
     L.blst_fr_fft_with_domain.restype = C.c_bool
     L.blst_fr_fft_with_domain.argtypes = [_vp, _sz, _vp, _sz, C.c_bool]
+    for f in ("catmsm_p1s_uncompress", "catmsm_p1s_deserialize"):
+        getattr(L, f).restype = C.c_int
+        getattr(L, f).argtypes = [_vp, _vp, _sz, _vp, C.c_int]
+    L.catmsm_p1s_affine_in_g1.restype = C.c_int
+    L.catmsm_p1s_affine_in_g1.argtypes = [_vp, _sz, _vp]
     L.catmsm_p1_fft_batch.restype = C.c_int
     L.catmsm_p1_fft_batch.argtypes = [_vp, _vp, _vp, _vp, _sz]
     L.catmsm_stream.restype = _vp
@@ -229,6 +234,24 @@ def fr_fft_with_domain(values: bytes, n: int, domain: bytes, domain_len: int, in
     ok = load().blst_fr_fft_with_domain(_buf(b) if b else None, n, _buf(domain) if domain else None,
                                         domain_len, inverse)
     return ok, bytes(b)
+
+
+def p1s_decode(encodings: bytes, n: int, compressed: bool, init: bytes = None, check_group=False):
+    """Batch uncompress (48-byte) / deserialize (96-byte) elements; returns
+    (rc, list of BLST_ERROR codes, affine outputs bytes)."""
+    L = load()
+    out = bytearray(init if init is not None else bytes(96 * n))
+    errs = (C.c_int * max(n, 1))()
+    f = L.catmsm_p1s_uncompress if compressed else L.catmsm_p1s_deserialize
+    rc = f(_buf(out), _buf(bytearray(encodings)), n, errs, 1 if check_group else 0)
+    return rc, list(errs)[:n], bytes(out)
+
+
+def p1s_affine_in_g1(points: bytes, n: int):
+    L = load()
+    res = (C.c_int * max(n, 1))()
+    rc = L.catmsm_p1s_affine_in_g1(_buf(bytearray(points)), n, res)
+    return rc, [bool(x) for x in list(res)[:n]]
 
 
 def p1_fft_batch(values_list, ns, domains, modes):
