@@ -113,6 +113,35 @@ bool blst_fr_fft(blst_fr *values, size_t n, bool inverse);
  * and scales by domain[n]; false before writing on a bad length or tag. */
 bool blst_fr_fft_with_domain(blst_fr *values, size_t n, const blst_fr *domain, size_t domain_len, bool inverse);
 
+/* Replaces blst_p1s_mult_wbits_precompute_sizeof (bindings/blst_scalar.h:527,
+ * blst/c_api.cpp:1310-1316 -> scalar/curve/multi_scalar.h:245-255):
+ * 96 * npoints * 2^(wbits-1); 0 for wbits outside [2, 14] or on overflow. */
+size_t blst_p1s_mult_wbits_precompute_sizeof(size_t wbits, size_t npoints);
+
+/* Replaces blst_p1s_mult_wbits_precompute (bindings/blst_scalar.h:529,
+ * blst/c_api.cpp:1318-1330 -> scalar/curve/multi_scalar.cpp:481-565): row i
+ * of the table is [P_i, 2 P_i, ..., 2^(wbits-1) P_i], affine, Montgomery,
+ * fully reduced, all-zero for infinity.  Invalid wbits, a NULL table or a
+ * NULL head with npoints != 0 return without writing.  Packed points may sit
+ * in the final npoints entries of the table: every point is read before the
+ * first table entry is written. */
+void blst_p1s_mult_wbits_precompute(blst_p1_affine table[], size_t wbits, const blst_p1_affine *const points[],
+                                    size_t npoints);
+
+/* Replaces blst_p1s_mult_wbits_scratch_sizeof (bindings/blst_scalar.h:531,
+ * blst/c_api.cpp:1332-1335 -> scalar/curve/multi_scalar.h:310-315):
+ * 144 * min(npoints, 8192); the GPU path does not touch the scratch. */
+size_t blst_p1s_mult_wbits_scratch_sizeof(size_t npoints);
+
+/* Replaces blst_p1s_mult_wbits (bindings/blst_scalar.h:533,
+ * blst/c_api.cpp:1337-1369 -> scalar/curve/multi_scalar.cpp:600-720):
+ * ret = sum_i k_i P_i over a table made by blst_p1s_mult_wbits_precompute;
+ * scalars as for blst_p1s_mult_pippenger.  npoints == 0 or nbits == 0 ->
+ * infinity; nbits > 256, wbits outside [2, 14], a NULL table, scalar head or
+ * scratch -> infinity.  Only the rows' first entries (the points) are read. */
+void blst_p1s_mult_wbits(blst_p1 *ret, const blst_p1_affine table[], size_t wbits, size_t npoints,
+                         const blst_byte *const scalars[], size_t nbits, blst_limb_t *scratch);
+
 /* ------------------------------------------------------------------ Part 2 */
 
 /* MSM over DEVICE-resident inputs (no reference counterpart): d_points is n

@@ -93,6 +93,14 @@ void oracle_p1s_tile_pippenger(op1 *ret, const op1a *const points[], size_t npoi
 void oracle_p1s_mult_naive(op1 *ret, const op1a *points, size_t npoints,
                            const uint8_t *scalars, size_t nbits);
 
+/* ---- fixed-table MSM (wbits.c): restates c_api.cpp:1310-1369,
+ *      multi_scalar.h:245-315, multi_scalar.cpp:481-720 ---- */
+size_t oracle_p1s_mult_wbits_precompute_sizeof(size_t wbits, size_t npoints);
+void oracle_p1s_mult_wbits_precompute(op1a *table, size_t wbits, const op1a *const points[], size_t npoints);
+size_t oracle_p1s_mult_wbits_scratch_sizeof(size_t npoints);
+void oracle_p1s_mult_wbits(op1 *ret, const op1a *table, size_t wbits, size_t npoints,
+                           const uint8_t *const scalars[], size_t nbits, uint64_t *scratch);
+
 /* ---- FFT (fft.c): restates fft_c_api.cpp:51-220, ctFft.h, domain.h ---- */
 size_t oracle_fr_fft_domain_len(size_t n);
 bool oracle_fr_fft_domain_init(ofr *domain, size_t domain_len, size_t n);

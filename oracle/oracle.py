@@ -61,6 +61,38 @@ class _Common:
         self._msm(_buf(ret), parr, n, sarr, nbits, scratch)
         return self.compress(bytes(ret))
 
+    def _bind_wbits(self, prefix):
+        L = self.L
+        f = lambda name: getattr(L, prefix + name)
+        f("p1s_mult_wbits_precompute_sizeof").restype = _sz
+        f("p1s_mult_wbits_precompute_sizeof").argtypes = [_sz, _sz]
+        f("p1s_mult_wbits_precompute").argtypes = [_vp, _sz, _vp, _sz]
+        f("p1s_mult_wbits_scratch_sizeof").restype = _sz
+        f("p1s_mult_wbits_scratch_sizeof").argtypes = [_sz]
+        f("p1s_mult_wbits").argtypes = [_vp, _vp, _sz, _sz, _vp, _sz, _vp]
+        self.wbits_table_sizeof = f("p1s_mult_wbits_precompute_sizeof")
+        self.wbits_scratch_sizeof = f("p1s_mult_wbits_scratch_sizeof")
+        self._wpre = f("p1s_mult_wbits_precompute")
+        self._wmsm = f("p1s_mult_wbits")
+
+    def wbits_table(self, points: bytes, n: int, wbits: int) -> bytes:
+        """Contiguous-descriptor table precompute; returns the table bytes."""
+        size = self.wbits_table_sizeof(wbits, n)
+        table = bytearray(size)
+        pbuf = _buf(bytearray(points))
+        parr = (C.c_void_p * 2)(C.cast(pbuf, C.c_void_p), None)
+        self._wpre(_buf(table), wbits, parr, n)
+        return bytes(table)
+
+    def wbits_msm(self, table: bytes, wbits: int, n: int, scalars: bytes, nbits: int = 255) -> bytes:
+        """Contiguous-descriptor fixed-table MSM; returns the compressed result."""
+        sbuf = _buf(bytearray(scalars))
+        sarr = (C.c_void_p * 2)(C.cast(sbuf, C.c_void_p), None)
+        scratch = (C.c_uint64 * max(1, self.wbits_scratch_sizeof(n) // 8))()
+        ret = bytearray(P1)
+        self._wmsm(_buf(ret), _buf(bytearray(table)), wbits, n, sarr, nbits, scratch)
+        return self.compress(bytes(ret))
+
 
 class Oracle(_Common):
     def __init__(self, path=ORACLE_SO):
@@ -110,6 +142,7 @@ class Oracle(_Common):
         L.ofr_from_mont.argtypes = [_vp, _vp]
         self._msm = L.oracle_p1s_mult_pippenger
         self.scratch_sizeof = L.oracle_p1s_mult_pippenger_scratch_sizeof
+        self._bind_wbits("oracle_")
         self.window_size = L.oracle_pippenger_window_size
 
     # ---- inputs ----
@@ -299,6 +332,7 @@ class Reference(_Common):
         L.blst_p1s_mult_pippenger_fr.argtypes = [_vp, _vp, _vp, _sz, _vp, _sz]
         self._msm = L.blst_p1s_mult_pippenger
         self.scratch_sizeof = L.blst_p1s_mult_pippenger_scratch_sizeof
+        self._bind_wbits("blst_")
 
     def compress(self, p: bytes) -> bytes:
         out = bytearray(48)

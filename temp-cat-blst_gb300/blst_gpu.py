@@ -125,6 +125,14 @@ def load(build_if_missing=True):
     L.catmsm_profile_entries.argtypes = []
     L.catmsm_profile_read.restype = C.c_int
     L.catmsm_profile_read.argtypes = [_vp, C.c_int, _vp]
+    L.blst_p1s_mult_wbits_precompute_sizeof.restype = _sz
+    L.blst_p1s_mult_wbits_precompute_sizeof.argtypes = [_sz, _sz]
+    L.blst_p1s_mult_wbits_precompute.restype = None
+    L.blst_p1s_mult_wbits_precompute.argtypes = [_vp, _sz, _vp, _sz]
+    L.blst_p1s_mult_wbits_scratch_sizeof.restype = _sz
+    L.blst_p1s_mult_wbits_scratch_sizeof.argtypes = [_sz]
+    L.blst_p1s_mult_wbits.restype = None
+    L.blst_p1s_mult_wbits.argtypes = [_vp, _vp, _sz, _sz, _vp, _sz, _vp]
     _lib = L
     return L
 
@@ -164,6 +172,47 @@ def p1s_mult_pippenger_descriptors(point_ptrs, scalar_ptrs, npoints, nbits, scra
         L.blst_p1s_mult_pippenger(_buf(ret), parr, npoints, sarr, nbits, scr)
     else:
         L.blst_p1s_mult_pippenger_window(_buf(ret), parr, npoints, sarr, nbits, scr, window)
+    return bytes(ret)
+
+
+def p1s_mult_wbits_precompute_sizeof(wbits: int, n: int) -> int:
+    return load().blst_p1s_mult_wbits_precompute_sizeof(wbits, n)
+
+
+def p1s_mult_wbits_scratch_sizeof(n: int) -> int:
+    return load().blst_p1s_mult_wbits_scratch_sizeof(n)
+
+
+def p1s_mult_wbits_precompute(points: bytes, n: int, wbits: int, table: bytearray = None,
+                              point_ptrs=None) -> bytes:
+    """Fixed-base table of n rows of 2^(wbits-1) affine multiples.  `table`
+    (optional) is the caller's buffer, written in place; `point_ptrs` an
+    optional explicit descriptor array (addresses or None) instead of the
+    contiguous `points`."""
+    L = load()
+    if table is None:
+        table = bytearray(max(96, L.blst_p1s_mult_wbits_precompute_sizeof(wbits, n)))
+    tb = _buf(table)
+    if point_ptrs is None:
+        pb = _buf(bytearray(points) if points else bytearray(96))
+        point_ptrs = [C.cast(pb, C.c_void_p).value, None]
+    parr = (C.c_void_p * len(point_ptrs))(*point_ptrs)
+    L.blst_p1s_mult_wbits_precompute(tb, wbits, parr, n)
+    return bytes(table)
+
+
+def p1s_mult_wbits(table: bytes, wbits: int, n: int, scalars: bytes, nbits: int = 255,
+                   scratch: bool = True, scalar_ptrs=None) -> bytes:
+    """Fixed-table MSM through the C ABI; returns the 144-byte blst_p1."""
+    L = load()
+    tb = _buf(bytearray(table) if table else bytearray(96))
+    if scalar_ptrs is None:
+        sb = _buf(bytearray(scalars) if scalars else bytearray(32))
+        scalar_ptrs = [C.cast(sb, C.c_void_p).value, None]
+    sarr = (C.c_void_p * len(scalar_ptrs))(*scalar_ptrs)
+    scr = (C.c_uint64 * 4)() if scratch else None
+    ret = bytearray(P1)
+    L.blst_p1s_mult_wbits(_buf(ret), tb if table is not None else None, wbits, n, sarr, nbits, scr)
     return bytes(ret)
 
 

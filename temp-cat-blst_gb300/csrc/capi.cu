@@ -57,26 +57,6 @@ static unsigned log2_exact(size_t n)
     return k;
 }
 
-// Gather the descriptor walk of multi_scalar.cpp:830-841 into contiguous
-// host staging; returns the contiguous base directly when possible.
-template <typename T>
-static const uint8_t* gather(const T* const arr[], size_t n, size_t elem, PinnedBuf& stage, bool& err)
-{
-    err = false;
-    if (n == 1 || arr[1] == nullptr) return reinterpret_cast<const uint8_t*>(arr[0]);
-    uint8_t* dst = (uint8_t*)stage.get(n * elem);
-    if (!dst) { err = true; return nullptr; }
-    const uint8_t* cur = reinterpret_cast<const uint8_t*>(arr[0]);
-    const T* const* next = arr + 1;
-    std::memcpy(dst, cur, elem);
-    for (size_t i = 1; i < n; i++) {
-        if (*next) cur = reinterpret_cast<const uint8_t*>(*next++);
-        else cur += elem;
-        std::memcpy(dst + i * elem, cur, elem);
-    }
-    return dst;
-}
-
 static void write_inf(blst_p1* ret) { std::memset(ret, 0, sizeof(*ret)); }
 
 static void msm_entry(blst_p1* ret, const blst_p1_affine* const points[], size_t npoints,

@@ -3,6 +3,7 @@
 // error helpers.  All public entry points are synchronous and fail closed.
 #pragma once
 #include <cuda_runtime.h>
+#include <cstring>
 #include <cstddef>
 #include <cstdint>
 #include <cstdio>
@@ -105,5 +106,25 @@ extern thread_local LaunchStats g_stats;
     } while (0)
 
 inline unsigned div_up(size_t a, size_t b) { return (unsigned)((a + b - 1) / b); }
+
+// Gather the descriptor walk of multi_scalar.cpp:830-841 into contiguous
+// host staging; returns the contiguous base directly when possible.
+template <typename T>
+inline const uint8_t* gather(const T* const arr[], size_t n, size_t elem, PinnedBuf& stage, bool& err)
+{
+    err = false;
+    if (n == 1 || arr[1] == nullptr) return reinterpret_cast<const uint8_t*>(arr[0]);
+    uint8_t* dst = (uint8_t*)stage.get(n * elem);
+    if (!dst) { err = true; return nullptr; }
+    const uint8_t* cur = reinterpret_cast<const uint8_t*>(arr[0]);
+    const T* const* next = arr + 1;
+    std::memcpy(dst, cur, elem);
+    for (size_t i = 1; i < n; i++) {
+        if (*next) cur = reinterpret_cast<const uint8_t*>(*next++);
+        else cur += elem;
+        std::memcpy(dst + i * elem, cur, elem);
+    }
+    return dst;
+}
 
 }  // namespace catmsm

@@ -12,6 +12,10 @@ reference's own C ABI built from its sources (oracle/_ref/libblst_ref.so):
   * domain: blst_fr_fft_domain_init bytes (sha256) per size
   * msm_fr: blst_p1s_mult_pippenger_fr (Montgomery Fr scalars) -> compressed
   * fr_fft: blst_fr_fft / blst_fr_fft_with_domain output bytes (sha256)
+  * wbits:  blst_p1s_mult_wbits_precompute table bytes (sha256) and
+            blst_p1s_mult_wbits -> compressed, per (n, wbits, nbits)
+
+`--section wbits` regenerates only that section of an existing file.
 """
 import hashlib
 import json
@@ -36,10 +40,51 @@ def msm_inputs(o, seed, n, kind, nbits, dup):
     return pts, packed
 
 
+def wbits_inputs(o, seed, n, kind, nbits, dup, inf):
+    """Seeded points (optionally with duplicates and one point at infinity,
+    index seed % n) and packed ceil(nbits/8)-byte scalars."""
+    pts, sc = msm_inputs(o, seed, n, kind, nbits, dup)
+    if inf:
+        k = seed % n
+        pts = pts[:96 * k] + bytes(96) + pts[96 * (k + 1):]
+    return pts, sc
+
+
+WBITS_CASES = [
+    # (seed, n, wbits, kind, nbits, dup, inf)
+    (61, 1, 2, 0, 255, False, False), (62, 5, 2, 0, 255, False, False),
+    (63, 17, 3, 0, 255, False, True), (64, 100, 4, 1, 64, False, True),
+    (65, 256, 8, 2, 255, True, False), (66, 33, 14, 0, 255, False, False),
+    (67, 1000, 6, 0, 256, False, True), (68, 4096, 5, 0, 255, False, False),
+    (69, 9, 10, 0, 7, False, False), (70, 8193, 3, 0, 255, False, True),
+    (71, 300, 7, 0, 17, True, True), (72, 2, 13, 0, 128, False, False),
+]
+
+
+def wbits_section(o, r):
+    out = []
+    for seed, n, w, kind, nbits, dup, inf in WBITS_CASES:
+        t = time.time()
+        pts, sc = wbits_inputs(o, seed, n, kind, nbits, dup, inf)
+        table = r.wbits_table(pts, n, w)
+        assert len(table) == 96 * n << (w - 1)
+        res = r.wbits_msm(table, w, n, sc, nbits)
+        out.append({"seed": seed, "n": n, "wbits": w, "kind": kind, "nbits": nbits, "dup": dup, "inf": inf,
+                    "table_sha256": hashlib.sha256(table).hexdigest(), "compressed": res.hex()})
+        print("wbits", seed, n, w, nbits, res.hex()[:16], "%.1fs" % (time.time() - t), flush=True)
+    return out
+
+
 def main():
     large = "--large" in sys.argv
     build(ref=True)
     o, r = Oracle(), Reference()
+    if "--section" in sys.argv and sys.argv[sys.argv.index("--section") + 1] == "wbits":
+        g = json.load(open(OUT))
+        g["wbits"] = wbits_section(o, r)
+        json.dump(g, open(OUT, "w"), indent=1)
+        print("wrote", OUT)
+        return
     g = {"msm": [], "fft": [], "domain": []}
     cases = [
         # (seed, n, kind, nbits, dup)
@@ -116,6 +161,7 @@ def main():
             assert ok
             g["fr_fft"].append({"seed": seed, "n": n, "mode": mode, "sha256": hashlib.sha256(out).hexdigest()})
         print("fr_fft", seed, n, flush=True)
+    g["wbits"] = wbits_section(o, r)
     if not large and os.path.exists(OUT):
         # keep previously generated large cases
         old = json.load(open(OUT))

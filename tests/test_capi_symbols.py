@@ -48,3 +48,15 @@ def test_scratch_sizeof_matches_reference_contract(gpu_binding, oracle):
         assert gpu_binding.fr_fft_domain_len(n) == 0
     for k in (0, 1, 10, 30):
         assert gpu_binding.fr_fft_domain_len(1 << k) == (1 << k) + 2
+
+
+def test_wbits_sizes_match_reference_contract(gpu_binding, oracle):
+    # pure host functions: no device call; values probed from the reference
+    for w in (0, 1, 2, 3, 8, 14, 15, 16, 64):
+        for n in (0, 1, 10, 4096, 1 << 40, 1 << 60):
+            assert gpu_binding.p1s_mult_wbits_precompute_sizeof(w, n) == oracle.wbits_table_sizeof(w, n), (w, n)
+    assert gpu_binding.p1s_mult_wbits_precompute_sizeof(2, 10) == 1920
+    assert gpu_binding.p1s_mult_wbits_precompute_sizeof(14, 10) == 96 * 10 * 8192
+    assert gpu_binding.p1s_mult_wbits_precompute_sizeof(15, 10) == 0
+    for n in (0, 1, 4096, 8191, 8192, 8193, 1 << 20):
+        assert gpu_binding.p1s_mult_wbits_scratch_sizeof(n) == oracle.wbits_scratch_sizeof(n) == 144 * min(n, 8192)

@@ -172,3 +172,71 @@ def test_oracle_fr_fft_matches_golden(golden, oracle):
         else:
             ok, out = oracle.fr_fft_with_domain(vals, n, d, n + 2, c["mode"] == "dinv")
         assert ok and hashlib.sha256(out).hexdigest() == c["sha256"], (n, c["mode"])
+
+
+def _wbits_inputs(oracle, c):
+    """Inputs of a golden wbits case: seeded points (duplicates, one point at
+    infinity at index seed % n, as flagged) and packed scalars."""
+    pts, sc = _msm_inputs(oracle, c)
+    if c["inf"]:
+        k = c["seed"] % c["n"]
+        pts = pts[:96 * k] + bytes(96) + pts[96 * (k + 1):]
+    return pts, sc
+
+
+def test_oracle_wbits_matches_golden(golden, oracle):
+    cases = golden["wbits"]
+    assert len(cases) >= 12
+    for c in cases:
+        if c["n"] << (c["wbits"] - 1) > 40000:
+            continue
+        pts, sc = _wbits_inputs(oracle, c)
+        table = oracle.wbits_table(pts, c["n"], c["wbits"])
+        assert hashlib.sha256(table).hexdigest() == c["table_sha256"], c
+        assert oracle.wbits_msm(table, c["wbits"], c["n"], sc, c["nbits"]).hex() == c["compressed"], c
+
+
+@pytest.mark.skipif(not om.reference_available(), reason="reference library not built here")
+def test_oracle_wbits_matches_reference_edge_cases(oracle):
+    """Packed points in the table's tail, explicit descriptor arrays and the
+    fail-closed cases, oracle vs the reference's own C ABI."""
+    ref = om.Reference()
+    n, w = 7, 4
+    m = 1 << (w - 1)
+    pts = oracle.gen_points(77, n)
+    sc = oracle.gen_scalars(78, n, 0)
+    exp = ref.wbits_table(pts, n, w)
+    assert oracle.wbits_table(pts, n, w) == exp
+    for lib in (oracle, ref):
+        pre = getattr(lib.L, "oracle_p1s_mult_wbits_precompute" if lib is oracle else "blst_p1s_mult_wbits_precompute")
+        table = bytearray(96 * n * m)
+        table[-96 * n:] = pts                       # packed input in the tail
+        tb = (C.c_char * len(table)).from_buffer(table)
+        parr = (C.c_void_p * 2)(C.addressof(tb) + len(table) - 96 * n, None)
+        pre(tb, w, parr, n)
+        assert bytes(table) == exp
+        # invalid wbits / NULL head: the table is left untouched
+        for bad_w, head in ((1, True), (15, True), (4, False)):
+            junk = bytearray(b"\x5a" * len(table))
+            jb = (C.c_char * len(junk)).from_buffer(junk)
+            parr = (C.c_void_p * 2)(C.addressof(tb) if head else None, None)
+            pre(jb, bad_w, parr, n)
+            assert bytes(junk) == b"\x5a" * len(table)
+    # explicit scalar descriptors in shuffled order
+    order = [4, 0, 6, 2, 1, 5, 3]
+    sb = (C.c_char * len(sc)).from_buffer(bytearray(sc))
+    sarr = (C.c_void_p * n)(*[C.addressof(sb) + 32 * i for i in order])
+    pshuf = b"".join(pts[96 * i:96 * i + 96] for i in order)
+    tshuf = ref.wbits_table(pshuf, n, w)
+    tb2 = (C.c_char * len(tshuf)).from_buffer(bytearray(tshuf))
+    scratch = (C.c_uint64 * 2048)()
+    r1, r2 = bytearray(144), bytearray(144)
+    oracle.L.oracle_p1s_mult_wbits((C.c_char * 144).from_buffer(r1), tb2, w, n, sarr, 255, scratch)
+    ref.L.blst_p1s_mult_wbits((C.c_char * 144).from_buffer(r2), tb2, w, n, sarr, 255, scratch)
+    assert oracle.compress(bytes(r1)) == ref.compress(bytes(r2)) == ref.msm(pts, sc, n, 255)
+    # fail-closed: NULL scratch, wbits 15, nbits 257 -> infinity
+    inf = bytes([0xC0]) + bytes(47)
+    for args in ((w, 255, None), (15, 255, scratch), (w, 257, scratch)):
+        oracle.L.oracle_p1s_mult_wbits((C.c_char * 144).from_buffer(r1), tb2, args[0], n, sarr, args[1], args[2])
+        ref.L.blst_p1s_mult_wbits((C.c_char * 144).from_buffer(r2), tb2, args[0], n, sarr, args[1], args[2])
+        assert oracle.compress(bytes(r1)) == ref.compress(bytes(r2)) == inf
