@@ -496,6 +496,12 @@ def run_ours(args, ws, rank, local):
     g.load()
     n = args.n
     dev = torch.device("cuda", local)
+    if args.only:
+        # one section alone (a diagnostic line, e.g. for an ncu launch list)
+        peak = max(g.imad_peak_forms())
+        fn = {"batched": batched_section, "fft": batched_fft_section}[args.only]
+        print(json.dumps({"section": args.only, args.only: fn(g, synth, torch, dev, args.steps, args.warmup, peak)}))
+        return 0
 
     # ---- seeded inputs, resident in HBM
     k_pts = torch.frombuffer(bytearray(synth.point_scalars(SEED, n)), dtype=torch.uint8).to(dev)
@@ -512,8 +518,7 @@ def run_ours(args, ws, rank, local):
     h_sc.copy_(d_sc.cpu())
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     stream = torch.cuda.ExternalStream(g.stream_handle(), device=dev)
-    c = g.msm_window(n)
-    D = NBITS // c + 1
+    c, D, npipe = g.msm_plan(n, NBITS)
 
     def barrier():
         if dist is not None:
@@ -522,7 +527,7 @@ def run_ours(args, ws, rank, local):
 
     if args.window:
         c = args.window
-        D = NBITS // c + 1
+        D = (127 if npipe == 2 * n else NBITS) // c + 1
 
     def step_device():
         return g.msm_device(d_pts.data_ptr(), d_sc.data_ptr(), 32, n, NBITS, args.window)
@@ -619,6 +624,7 @@ def run_ours(args, ws, rank, local):
         "data": "synthetic (seeded: P_i = k_i G, uniform Fr scalars)",
         "config": {"workload": "G1 MSM n=2^20, uniform 255-bit Fr scalars, 96-B affine points",
                    "n": n, "nbits": NBITS, "window_c": c, "windows": D,
+                   "glv_split": npipe == 2 * n, "pipeline_points": npipe,
                    "l2": "L2 flushed (256 MB write) between steps; inputs 134 MB + working set > L2",
                    "parallelism": "replicas" if ws > 1 else "single"},
         "e2e": {"value": aggregate_mpoints(ws, n, e2e_ms), "unit": UNIT,
@@ -679,6 +685,8 @@ def main():
     ap.add_argument("--window", type=int, default=0, help="MSM window width (0 = library default)")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched MSM / FFT sections")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving sweep")
+    ap.add_argument("--only", choices=["batched", "fft"], default=None,
+                    help="run only the batched-commitments or batched-FFT section (diagnostic line)")
     ap.add_argument("--serve-rates", default="25,50,100,150", help="Poisson arrival rates (requests/s)")
     ap.add_argument("--serve-seconds", type=float, default=3.0, help="arrival window per rate")
     args = ap.parse_args()

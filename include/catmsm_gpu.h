@@ -145,14 +145,15 @@ void blst_p1s_mult_wbits(blst_p1 *ret, const blst_p1_affine table[], size_t wbit
 /* ------------------------------------------------------------------ Part 2 */
 
 /* MSM over DEVICE-resident inputs (no reference counterpart): d_points is n
- * contiguous affine points, d_scalars n scalars of `stride` bytes (nbits used),
- * all in device memory of the current device; window 0 = library default.
+ * contiguous affine points (16-byte aligned), d_scalars n scalars of `stride`
+ * bytes (nbits used), all in device memory of the current device; window 0 =
+ * library default.
  * Runs on the calling thread's library stream; the result lands in host *ret.
  * Returns 0 on success, else a cudaError_t value (ret set to infinity). */
 int catmsm_p1s_mult_pippenger_device(blst_p1 *ret, const void *d_points, const void *d_scalars,
                                      size_t stride, size_t npoints, size_t nbits, size_t window);
 
-/* G1 FFT over DEVICE-resident Jacobian values with a DEVICE-resident domain
+/* G1 FFT over DEVICE-resident Jacobian values (16-byte aligned) with a DEVICE-resident domain
  * (n + 2 Montgomery Fr, as built by blst_fr_fft_domain_init).  mode 0:
  * forward, 1: inverse (scaled), 2: inverse unscaled.  Returns 0 on success. */
 int catmsm_p1_fft_device(void *d_values, size_t n, const void *d_domain, int mode);
@@ -174,8 +175,21 @@ void *catmsm_stream(void);
 /* Number of kernels this thread launched through the library so far. */
 long catmsm_launch_count(void);
 
-/* The window width the GPU MSM uses for n points. */
+/* The window width the GPU MSM uses for n points of scalars of at most 128
+ * bits (no GLV split). */
 size_t catmsm_msm_window(size_t npoints);
+
+/* The plan of the calling thread's next MSM of n points with nbits-bit
+ * scalars: window width, number of windows, and the number of points the
+ * pipeline runs over (2n when the GLV split applies: nbits > 128 and the
+ * split enabled).  Returns 0, or -1 on invalid arguments. */
+int catmsm_msm_plan(size_t npoints, size_t nbits, size_t *window, size_t *windows, size_t *points);
+
+/* Enables (1) or disables (0) the GLV split for the calling thread's MSMs
+ * (on by default; -1 only queries).  Returns the previous setting, or -1
+ * without a device context.  Both settings give the same group element for
+ * subgroup points, the reference's precondition. */
+int catmsm_msm_glv(int enable);
 
 /* Seeded-input support: out[i] = k_i * G (affine, canonical) for n 32-byte
  * little-endian scalars.  Host buffers; returns 0 on success. */
@@ -288,7 +302,8 @@ int catmsm_p1s_deserialize(blst_p1_affine *out, const blst_byte *in96, size_t n,
 int catmsm_p1s_affine_in_g1(const blst_p1_affine *points, size_t n, int *results);
 
 /* Field self-check: out[i] = a[i] * b[i] * R^-1 mod p (canonical), host
- * buffers of n blst_fp.  Returns 0 on success. */
+ * buffers of n blst_fp with inputs below 2p; a == b (the same pointer)
+ * selects the dedicated squaring.  Returns 0 on success. */
 int catmsm_fp_mul(blst_fp *out, const blst_fp *a, const blst_fp *b, size_t n);
 
 #ifdef __cplusplus

@@ -83,6 +83,10 @@ def load(build_if_missing=True):
     L.catmsm_launch_count.argtypes = []
     L.catmsm_msm_window.restype = _sz
     L.catmsm_msm_window.argtypes = [_sz]
+    L.catmsm_msm_plan.restype = C.c_int
+    L.catmsm_msm_plan.argtypes = [_sz, _sz, _vp, _vp, _vp]
+    L.catmsm_msm_glv.restype = C.c_int
+    L.catmsm_msm_glv.argtypes = [C.c_int]
     L.catmsm_p1_affines_from_scalars.restype = C.c_int
     L.catmsm_p1_affines_from_scalars.argtypes = [_vp, _vp, _sz]
     L.catmsm_p1_affines_from_scalars_device.restype = C.c_int
@@ -361,7 +365,19 @@ def msm_window(n: int) -> int:
     return load().catmsm_msm_window(n)
 
 
-STAGES = ("memset", "digits", "scan", "scatter", "accumulate", "fixup", "reduce", "host_fold")
+STAGES = ("prep", "digits", "scan", "scatter", "accumulate", "fixup", "reduce", "host_fold")
+
+
+def msm_plan(n: int, nbits: int = 255):
+    """(window, windows, pipeline points) of this thread's next MSM."""
+    c, d, p = _sz(), _sz(), _sz()
+    assert load().catmsm_msm_plan(n, nbits, C.byref(c), C.byref(d), C.byref(p)) == 0
+    return c.value, d.value, p.value
+
+
+def msm_glv(enable: int = -1) -> int:
+    """Set (0/1) or query (-1) the GLV split for this thread; returns the previous setting."""
+    return load().catmsm_msm_glv(enable)
 
 
 def imad_peak_tera() -> float:

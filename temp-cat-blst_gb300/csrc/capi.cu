@@ -316,7 +316,9 @@ int catmsm_p1s_mult_pippenger_device(blst_p1* ret, const void* d_points, const v
     if (!ret) return (int)cudaErrorInvalidValue;
     write_inf(ret);
     if (npoints == 0 || nbits == 0) return 0;
-    if (!d_points || !d_scalars || nbits > 256 || stride < (nbits + 7) / 8 || window > 24) return (int)cudaErrorInvalidValue;
+    if (!d_points || !d_scalars || nbits > 256 || stride < (nbits + 7) / 8 || window > 24 ||
+        (reinterpret_cast<uintptr_t>(d_points) & 15) != 0)
+        return (int)cudaErrorInvalidValue;
     Ctx* ctx = get_ctx();
     if (!ctx) return (int)cudaErrorInitializationError;
     uint64_t out[18];
@@ -329,7 +331,9 @@ int catmsm_p1s_mult_pippenger_device(blst_p1* ret, const void* d_points, const v
 
 int catmsm_p1_fft_device(void* d_values, size_t n, const void* d_domain, int mode)
 {
-    if (!d_values || !d_domain || !valid_fft_size(n) || mode < 0 || mode > 2) return (int)cudaErrorInvalidValue;
+    if (!d_values || !d_domain || !valid_fft_size(n) || mode < 0 || mode > 2 ||
+        (reinterpret_cast<uintptr_t>(d_values) & 15) != 0)
+        return (int)cudaErrorInvalidValue;
     Ctx* ctx = get_ctx();
     if (!ctx) return (int)cudaErrorInitializationError;
     const uint32_t* dr = (const uint32_t*)d_domain;
@@ -347,6 +351,28 @@ void* catmsm_stream(void)
 long catmsm_launch_count(void) { return g_stats.launches; }
 
 size_t catmsm_msm_window(size_t npoints) { return msm_default_window(npoints); }
+
+int catmsm_msm_glv(int enable)
+{
+    Ctx* ctx = get_ctx();
+    if (!ctx) return -1;
+    const int prev = ctx->glv ? 1 : 0;
+    if (enable >= 0) ctx->glv = enable != 0;
+    return prev;
+}
+
+int catmsm_msm_plan(size_t npoints, size_t nbits, size_t* window, size_t* windows, size_t* points)
+{
+    Ctx* ctx = get_ctx();
+    if (!ctx || npoints == 0 || nbits == 0 || nbits > 256 || !window || !windows || !points) return -1;
+    uint32_t c, D;
+    size_t np;
+    msm_plan(ctx, npoints, (uint32_t)nbits, &c, &D, &np);
+    *window = c;
+    *windows = D;
+    *points = np;
+    return 0;
+}
 
 int catmsm_p1_affines_from_scalars_device(void* d_out, const void* d_k32, size_t n)
 {
@@ -383,7 +409,7 @@ int catmsm_fp_mul(blst_fp* out, const blst_fp* a, const blst_fp* b, size_t n)
     if (!d) return (int)cudaErrorMemoryAllocation;
     cudaError_t err = cudaMemcpyAsync(d, a, n * sizeof(blst_fp), cudaMemcpyHostToDevice, ctx->stream);
     if (err == cudaSuccess) err = cudaMemcpyAsync(d + 6 * n, b, n * sizeof(blst_fp), cudaMemcpyHostToDevice, ctx->stream);
-    if (err == cudaSuccess) err = fp_mul_test_device(ctx, d, d + 6 * n, d + 12 * n, n);
+    if (err == cudaSuccess) err = fp_mul_test_device(ctx, d, d + 6 * n, d + 12 * n, n, a == b);
     if (err == cudaSuccess)
         err = cudaMemcpyAsync(out, d + 12 * n, n * sizeof(blst_fp), cudaMemcpyDeviceToHost, ctx->stream);
     if (err == cudaSuccess) err = cudaStreamSynchronize(ctx->stream);

@@ -20,12 +20,18 @@ size_t basis_points(const Basis* b);
 uint32_t basis_window(const Basis* b);
 int basis_device(const Basis* b);
 
+// Window width, window count and pipeline point count msm_device uses for
+// n points of nbits-bit scalars on this context (2n points of 127 bits when
+// the GLV split applies).
+void msm_plan(const Ctx* ctx, size_t n, uint32_t nbits, uint32_t* c, uint32_t* windows, size_t* points);
+
 cudaError_t msm_device(Ctx* ctx, const void* d_points, const uint8_t* d_scalars, uint32_t stride,
                        size_t n, uint32_t nbits, uint32_t c, uint64_t* out);
 
 cudaError_t points_from_scalars_device(Ctx* ctx, const uint8_t* d_k32, size_t n, void* d_out);
 
-cudaError_t fp_mul_test_device(Ctx* ctx, const uint64_t* d_a, const uint64_t* d_b, uint64_t* d_out, size_t n);
+cudaError_t fp_mul_test_device(Ctx* ctx, const uint64_t* d_a, const uint64_t* d_b, uint64_t* d_out, size_t n,
+                               bool square);
 
 // One transform of a batch: n points, the n Montgomery roots its butterflies
 // index, whether the inverse reads forward roots at n - idx, and an optional

@@ -57,7 +57,7 @@ __device__ __forceinline__ void fp_set_one(fp& r)
 }
 
 // r = a * b * 2^-384 mod p; inputs in [0, 2p), output in [0, 2p).
-__device__ __forceinline__ void fp_mul(fp& r, const fp& a, const fp& b)
+__device__ __forceinline__ void fp_mul_impl(fp& r, const fp& a, const fp& b)
 {
     uint32_t t[12];
     uint32_t e[13], o[13];
@@ -158,6 +158,21 @@ __device__ __forceinline__ void fp_mul(fp& r, const fp& a, const fp& b)
 #pragma unroll
     for (int k = 0; k < 12; k++) r.v[k] = t[k];
 }
+
+// The multiplication is one out-of-line function per translation unit, called
+// with its operands and result in registers.  Inlined, a group operation is
+// ~10 copies of ~750 instructions and the accumulation loop outgrows the
+// instruction cache (ncu: ~2 cycles of no_instruction stall per issue); out of
+// line the hot loop is one body plus call sites.  Measured on GB300: the 2^20
+// MSM 9.1 -> 8.0 ms, a 2^14 G1 FFT 39 -> 26 ms.
+static __device__ __noinline__ fp fp_mul_call(const fp a, const fp b)
+{
+    fp r;
+    fp_mul_impl(r, a, b);
+    return r;
+}
+
+__device__ __forceinline__ void fp_mul(fp& r, const fp& a, const fp& b) { r = fp_mul_call(a, b); }
 
 __device__ __forceinline__ void fp_sqr(fp& r, const fp& a) { fp_mul(r, a, a); }
 

@@ -117,15 +117,61 @@ __device__ __forceinline__ void fr_pow_u32(uint32_t* o, const uint32_t* base, ui
     for (int i = 0; i < 8; i++) o[i] = acc[i];
 }
 
-// GLV split of a canonical k < r: k = k1 + lambda * k2, 0 <= k1 < lambda, k2 <= lambda + 1
-// (binary long division; both halves fit 128 bits).
+// floor(2^256 / lambda), 129 bits, little-endian words
+__device__ __constant__ static const uint32_t FR_LAMBDA_MU[5] = {0xf6cfee30u, 0x63f6e522u, 0xe01faaddu, 0x7c6becf1u,
+                                                                 0x00000001u};
+
+// GLV split of a canonical k < r: k = k1 + lambda * k2, 0 <= k1 < lambda,
+// k2 = floor(k / lambda) <= lambda + 1 (both fit 128 bits).  Barrett
+// quotient q = floor(floor(k / 2^127) * mu / 2^129) with mu = floor(2^256 /
+// lambda) is at most two below floor(k / lambda); the remainder is corrected
+// by at most two subtractions.
 __device__ __forceinline__ void fr_glv_split(uint32_t* k1, uint32_t* k2, const uint32_t* k)
 {
-    uint32_t rem[5] = {0, 0, 0, 0, 0};
-    uint32_t q[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    for (int i = 255; i >= 0; i--) {
-        for (int w = 4; w > 0; w--) rem[w] = (rem[w] << 1) | (rem[w - 1] >> 31);
-        rem[0] = (rem[0] << 1) | ((k[i >> 5] >> (i & 31)) & 1);
+    uint32_t a[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) a[i] = (k[i + 3] >> 31) | (k[i + 4] << 1);   // k >> 127 (k < 2^255)
+    uint32_t prod[9];
+#pragma unroll
+    for (int i = 0; i < 9; i++) prod[i] = 0;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        uint64_t c = 0;
+#pragma unroll
+        for (int j = 0; j < 5; j++) {
+            c += (uint64_t)a[i] * FR_LAMBDA_MU[j] + prod[i + j];
+            prod[i + j] = (uint32_t)c;
+            c >>= 32;
+        }
+        prod[i + 5] = (uint32_t)c;
+    }
+    uint32_t q[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) q[i] = (prod[i + 4] >> 1) | (prod[i + 5] << 31);   // >> 129
+    // rem = k - q * lambda (< 3 lambda: five words)
+    uint32_t t[8];
+#pragma unroll
+    for (int i = 0; i < 8; i++) t[i] = 0;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        uint64_t c = 0;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            c += (uint64_t)q[i] * FR_LAMBDA[j] + t[i + j];
+            t[i + j] = (uint32_t)c;
+            c >>= 32;
+        }
+        t[i + 4] = (uint32_t)c;
+    }
+    uint32_t rem[5];
+    uint64_t br = 0;
+#pragma unroll
+    for (int i = 0; i < 5; i++) {
+        const uint64_t d = (uint64_t)k[i] - t[i] - br;
+        rem[i] = (uint32_t)d;
+        br = (d >> 63) & 1;
+    }
+    for (int it = 0; it < 3; it++) {
         bool ge = rem[4] != 0;
         if (!ge) {
             ge = true;
@@ -133,17 +179,18 @@ __device__ __forceinline__ void fr_glv_split(uint32_t* k1, uint32_t* k2, const u
                 if (rem[w] != FR_LAMBDA[w]) { ge = rem[w] > FR_LAMBDA[w]; break; }
             }
         }
-        if (ge) {
-            uint64_t br = 0;
-            for (int w = 0; w < 4; w++) {
-                uint64_t d = (uint64_t)rem[w] - FR_LAMBDA[w] - br;
-                rem[w] = (uint32_t)d;
-                br = (d >> 63) & 1;
-            }
-            rem[4] -= (uint32_t)br;
-            q[i >> 5] |= 1u << (i & 31);
+        if (!ge) break;
+        br = 0;
+#pragma unroll
+        for (int w = 0; w < 4; w++) {
+            const uint64_t d = (uint64_t)rem[w] - FR_LAMBDA[w] - br;
+            rem[w] = (uint32_t)d;
+            br = (d >> 63) & 1;
         }
+        rem[4] -= (uint32_t)br;
+        for (int w = 0; w < 4 && ++q[w] == 0; w++) {}
     }
+#pragma unroll
     for (int w = 0; w < 4; w++) { k1[w] = rem[w]; k2[w] = q[w]; }
 }
 

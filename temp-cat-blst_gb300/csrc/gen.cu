@@ -95,20 +95,23 @@ cudaError_t points_from_scalars_device(Ctx* ctx, const uint8_t* d_k32, size_t n,
     return cudaGetLastError();
 }
 
-__global__ void k_fp_mul_test(const fp* __restrict__ a, const fp* __restrict__ b, fp* __restrict__ o, uint32_t n)
+__global__ void k_fp_mul_test(const fp* __restrict__ a, const fp* __restrict__ b, fp* __restrict__ o, uint32_t n,
+                              int square)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     fp x = a[i], y = b[i], r;
-    fp_mul(r, x, y);
+    if (square) fp_sqr(r, x);
+    else fp_mul(r, x, y);
     fp_canon(r, r);
     o[i] = r;
 }
 
-cudaError_t fp_mul_test_device(Ctx* ctx, const uint64_t* d_a, const uint64_t* d_b, uint64_t* d_out, size_t n)
+cudaError_t fp_mul_test_device(Ctx* ctx, const uint64_t* d_a, const uint64_t* d_b, uint64_t* d_out, size_t n,
+                               bool square)
 {
     k_fp_mul_test<<<div_up(n, 128), 128, 0, ctx->stream>>>((const fp*)d_a, (const fp*)d_b, (fp*)d_out,
-                                                           (uint32_t)n);
+                                                           (uint32_t)n, square ? 1 : 0);
     g_stats.launches++;
     return cudaGetLastError();
 }

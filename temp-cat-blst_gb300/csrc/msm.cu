@@ -4,6 +4,13 @@
 // multi_scalar.cpp:806-923).  The result is the same group element
 // sum_i (k_i mod 2^nbits) * P_i; the device pipeline is:
 //
+//   0. k_glv_prep    (scalars wider than 128 bits) the GLV split: the points
+//                    are prime-order subgroup elements (the reference's
+//                    contract, blst_scalar.h:539), where phi(x, y) =
+//                    (beta x, y) = lambda P, so k P = s1 m1 P + s2 m2 phi(P)
+//                    with m1, m2 < 2^127: an n-point 255-bit MSM becomes a
+//                    2n-point 127-bit MSM with the same bucket entries and
+//                    half the windows to reduce and fold.
 //   1. k_digits      signed c-bit window digits (carry recoding, digit in
 //                    [-2^(c-1), 2^(c-1)]), one thread per scalar; each nonzero
 //                    digit takes a rank in its bucket with one atomicAdd.
@@ -24,9 +31,11 @@
 //                    (reference multi_scalar.cpp:913-922), then normalises.
 #include "common.cuh"
 #include "curve.cuh"
+#include "fr.cuh"
 #include "host_curve.hpp"
 #include "catmsm_internal.h"
 
+#include <cmath>
 #include <mutex>
 
 namespace catmsm {
@@ -57,6 +66,14 @@ __device__ __forceinline__ void store_xyzz(xyzz* dst, const xyzz& p)
     for (int k = 0; k < 12; k++) q[k] = make_uint4(s[4 * k], s[4 * k + 1], s[4 * k + 2], s[4 * k + 3]);
 }
 
+__device__ __forceinline__ void store_affine(affine* dst, const affine& p)
+{
+    uint4* q = reinterpret_cast<uint4*>(dst);
+    const uint32_t* s = reinterpret_cast<const uint32_t*>(&p);
+#pragma unroll
+    for (int k = 0; k < 6; k++) q[k] = make_uint4(s[4 * k], s[4 * k + 1], s[4 * k + 2], s[4 * k + 3]);
+}
+
 __device__ __forceinline__ void load_xyzz(xyzz& p, const xyzz* src)
 {
     const uint4* q = reinterpret_cast<const uint4*>(src);
@@ -69,22 +86,20 @@ __device__ __forceinline__ void load_xyzz(xyzz& p, const xyzz* src)
 }
 
 // ----------------------------------------------------------------- 1. digits
-__global__ void k_digits(const uint8_t* __restrict__ scalars, uint32_t stride, uint32_t n,
-                         uint32_t nbits, uint32_t c, uint32_t D, uint32_t* __restrict__ digits,
-                         uint32_t* __restrict__ ranks, uint32_t* __restrict__ counts)
+// k = the low nbits bits of a little-endian scalar of `stride` bytes
+__device__ __forceinline__ void load_scalar(uint32_t* k, const uint8_t* s, uint32_t stride, uint32_t nbits)
 {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    uint32_t k[9];
 #pragma unroll
-    for (int j = 0; j < 9; j++) k[j] = 0;
-    const uint8_t* s = scalars + (size_t)i * stride;
+    for (int j = 0; j < 8; j++) k[j] = 0;
     const uint32_t nbytes = (nbits + 7) >> 3;
     if (stride == 32 && (reinterpret_cast<uintptr_t>(s) & 15) == 0) {
         const uint4 a = __ldg(reinterpret_cast<const uint4*>(s));
         const uint4 b = __ldg(reinterpret_cast<const uint4*>(s) + 1);
         k[0] = a.x; k[1] = a.y; k[2] = a.z; k[3] = a.w;
         k[4] = b.x; k[5] = b.y; k[6] = b.z; k[7] = b.w;
+    } else if (stride == 16 && (reinterpret_cast<uintptr_t>(s) & 15) == 0) {
+        const uint4 a = __ldg(reinterpret_cast<const uint4*>(s));
+        k[0] = a.x; k[1] = a.y; k[2] = a.z; k[3] = a.w;
     } else {
         for (uint32_t b = 0; b < nbytes; b++) k[b >> 2] |= (uint32_t)s[b] << (8 * (b & 3));
     }
@@ -93,6 +108,103 @@ __global__ void k_digits(const uint8_t* __restrict__ scalars, uint32_t stride, u
         if (nbits <= 32 * j) k[j] = 0;
         else if (nbits < 32 * (j + 1)) k[j] &= (1u << (nbits - 32 * j)) - 1;
     }
+}
+
+// ----------------------------------------------------------------- 0. GLV split
+// (lambda + 1) / 2 and lambda + 1, little-endian words (lambda = z^2 - 1,
+// lambda^2 + lambda + 1 = r)
+__device__ __constant__ static const uint32_t GLV_HALF[4] = {0x80000000u, 0x00000000u, 0x8000d201u, 0x5622d200u};
+__device__ __constant__ static const uint32_t GLV_LAMBDA1[4] = {0x00000000u, 0x00000001u, 0x0001a402u, 0xac45a401u};
+
+__device__ __forceinline__ bool ge4(const uint32_t* a, const uint32_t* b)
+{
+    for (int i = 3; i >= 0; i--)
+        if (a[i] != b[i]) return a[i] > b[i];
+    return true;
+}
+
+__device__ __forceinline__ void sub4(uint32_t* o, const uint32_t* a, const uint32_t* b)
+{
+    uint64_t br = 0;
+    for (int i = 0; i < 4; i++) {
+        const uint64_t d = (uint64_t)a[i] - b[i] - br;
+        o[i] = (uint32_t)d;
+        br = (d >> 63) & 1;
+    }
+}
+
+__device__ __forceinline__ void inc4(uint32_t* a)
+{
+    for (int i = 0; i < 4 && ++a[i] == 0; i++) {}
+}
+
+__device__ __forceinline__ void dec4(uint32_t* a)
+{
+    for (int i = 0; i < 4 && a[i]-- == 0; i++) {}
+}
+
+// Thread i: k = k_i mod r = k1 + k2 lambda (0 <= k1 < lambda, k2 <= lambda + 1),
+// balanced to k = s1 m1 + s2 m2 lambda with m1, m2 <= (lambda + 1) / 2:
+//   k1 >= (lambda+1)/2:  k1 -> k1 - lambda,  k2 -> k2 + 1
+//   k2 >= (lambda+1)/2:  k2 -> k2 - lambda - 1,  k1 -> k1 - 1
+// (the second uses lambda^2 = -lambda - 1 mod r).  Writes the 16-byte
+// magnitudes m1 -> gsc[i], m2 -> gsc[n + i] and the signed points
+// s1 P -> gpts[i], s2 phi(P) -> gpts[n + i].
+__global__ void k_glv_prep(const affine* __restrict__ pts, const uint8_t* __restrict__ scalars, uint32_t stride,
+                           uint32_t n, uint32_t nbits, affine* __restrict__ gpts, uint4* __restrict__ gsc)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t k[8];
+    load_scalar(k, scalars + (size_t)i * stride, stride, nbits);
+    while (fr_geq(k, FR_R)) fr_sub_r(k);
+    uint32_t m1[4], m2[4];
+    fr_glv_split(m1, m2, k);
+    bool s1 = false, s2 = false;
+    if (ge4(m1, GLV_HALF)) {
+        sub4(m1, FR_LAMBDA, m1);
+        s1 = true;
+        inc4(m2);
+    }
+    if (ge4(m2, GLV_HALF)) {
+        sub4(m2, GLV_LAMBDA1, m2);
+        s2 = true;
+        if (s1) {
+            inc4(m1);
+        } else if ((m1[0] | m1[1] | m1[2] | m1[3]) == 0) {
+            m1[0] = 1;
+            s1 = true;
+        } else {
+            dec4(m1);
+        }
+    }
+    gsc[i] = make_uint4(m1[0], m1[1], m1[2], m1[3]);
+    gsc[n + i] = make_uint4(m2[0], m2[1], m2[2], m2[3]);
+    affine p;
+    load_affine(p.x, p.y, pts + i);
+    affine a = p, b = p;
+    if (!aff_is_inf(p)) {
+        fp beta;
+#pragma unroll
+        for (int w = 0; w < 12; w++) beta.v[w] = FP_BETA[w];
+        fp_mul(b.x, p.x, beta);
+        fp_canon(b.x, b.x);
+        if (s1) fp_neg(a.y, p.y);
+        if (s2) fp_neg(b.y, p.y);
+    }
+    store_affine(gpts + i, a);
+    store_affine(gpts + n + i, b);
+}
+
+__global__ void k_digits(const uint8_t* __restrict__ scalars, uint32_t stride, uint32_t n,
+                         uint32_t nbits, uint32_t c, uint32_t D, uint32_t* __restrict__ digits,
+                         uint32_t* __restrict__ ranks, uint32_t* __restrict__ counts)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t k[9];
+    load_scalar(k, scalars + (size_t)i * stride, stride, nbits);
+    k[8] = 0;
     const uint32_t B = 1u << (c - 1);
     const uint32_t cmask = (1u << c) - 1;
     uint32_t carry = 0;
@@ -223,7 +335,7 @@ __device__ __forceinline__ void madd_entry(xyzz& acc, const affine* __restrict__
     xyzz_madd(acc, x, y);
 }
 
-__global__ void __launch_bounds__(128) k_accumulate(const affine* __restrict__ pts,
+__global__ void __launch_bounds__(128, 4) k_accumulate(const affine* __restrict__ pts,
                                                     const uint32_t* __restrict__ sorted_pt,
                                                     const uint32_t* __restrict__ sorted_key,
                                                     const uint32_t* __restrict__ total_ptr, uint32_t L,
@@ -395,6 +507,41 @@ uint32_t msm_default_window(size_t n)
     return (uint32_t)c;
 }
 
+// Window for the GLV halves (n2 points of 127-bit scalars): among widths whose
+// top window keeps at least half of c bits (a narrow top window concentrates
+// its entries in a few hot buckets), the c in [2, 20] minimising bucket
+// entries + 4 x buckets (reducing a bucket costs about four accumulated
+// entries on this GPU).  Measured best: 16 for n2 = 2^21, 19 for n2 = 2^23.
+uint32_t msm_glv_window(size_t n2)
+{
+    double best = 0;
+    uint32_t bc = 0;
+    for (uint32_t c = 2; c <= 20; c++) {
+        const uint32_t D = 127 / c + 1;
+        const uint32_t top = 127 - (D - 1) * c;
+        if (2 * top < c) continue;
+        const double entries = (double)n2 * ((D - 1) + (1.0 - std::ldexp(1.0, -(int)top)));
+        const double cost = entries + 4.0 * D * std::ldexp(1.0, (int)c - 1);
+        if (bc == 0 || cost < best) { best = cost; bc = c; }
+    }
+    return bc;
+}
+
+static bool use_glv(const Ctx* ctx, size_t n, uint32_t nbits)
+{
+    return ctx->glv && nbits > 128 && n < (1u << 30);
+}
+
+void msm_plan(const Ctx* ctx, size_t n, uint32_t nbits, uint32_t* c, uint32_t* windows, size_t* points)
+{
+    const bool g = use_glv(ctx, n, nbits);
+    const size_t np = g ? 2 * n : n;
+    const uint32_t nb = g ? 127 : nbits;
+    *c = g ? msm_glv_window(np) : msm_default_window(np);
+    *windows = nb / *c + 1;
+    *points = np;
+}
+
 // Runs the device pipeline over device-resident points/scalars on the context
 // stream and returns the folded, normalised result in `out` (144 bytes).
 cudaError_t msm_device(Ctx* ctx, const void* d_points, const uint8_t* d_scalars, uint32_t stride,
@@ -402,8 +549,31 @@ cudaError_t msm_device(Ctx* ctx, const void* d_points, const uint8_t* d_scalars,
 {
     cudaStream_t st = ctx->stream;
     MsmWork& W = ctx->msm;
+    if (n == 0 || n > 0x7fffffffu) return cudaErrorInvalidValue;
+    StageProfile& P = ctx->prof;
+    if (P.enabled && !P.ev[0]) {
+        for (int i = 0; i <= kMsmStages; i++) CATMSM_CHECK(cudaEventCreate(&P.ev[i]));
+    }
+    auto mark = [&](int i) {
+        if (P.enabled) cudaEventRecord(P.ev[i], st);
+    };
+    mark(0);
+    if (use_glv(ctx, n, nbits)) {
+        affine* gpts = (affine*)W.glv_pts.get(2 * n * sizeof(affine));
+        uint4* gsc = (uint4*)W.glv_sc.get(2 * n * sizeof(uint4));
+        if (!gpts || !gsc) return cudaErrorMemoryAllocation;
+        k_glv_prep<<<div_up(n, 128), 128, 0, st>>>((const affine*)d_points, d_scalars, stride, (uint32_t)n, nbits,
+                                                   gpts, gsc);
+        g_stats.launches++;
+        d_points = gpts;
+        d_scalars = reinterpret_cast<const uint8_t*>(gsc);
+        stride = 16;
+        n *= 2;
+        nbits = 127;
+        if (c == 0) c = msm_glv_window(n);
+    }
     if (c == 0) c = msm_default_window(n);
-    if (c < 2 || c > 22 || n == 0 || n > 0x7fffffffu) return cudaErrorInvalidValue;
+    if (c < 2 || c > 22) return cudaErrorInvalidValue;
     const uint32_t D = nbits / c + 1;
     const uint32_t B = 1u << (c - 1);
     const size_t M = (size_t)D * B;
@@ -438,14 +608,6 @@ cudaError_t msm_device(Ctx* ctx, const void* d_points, const uint8_t* d_scalars,
         return cudaErrorMemoryAllocation;
     uint32_t* total = offsets + M;
 
-    StageProfile& P = ctx->prof;
-    if (P.enabled && !P.ev[0]) {
-        for (int i = 0; i <= kMsmStages; i++) CATMSM_CHECK(cudaEventCreate(&P.ev[i]));
-    }
-    auto mark = [&](int i) {
-        if (P.enabled) cudaEventRecord(P.ev[i], st);
-    };
-    mark(0);
     CATMSM_CHECK(cudaMemsetAsync(counts, 0, M * 4, st));
     CATMSM_CHECK(cudaMemsetAsync(buckets, 0, M * sizeof(xyzz), st));
     CATMSM_CHECK(cudaMemsetAsync(hot_count, 0, 4, st));

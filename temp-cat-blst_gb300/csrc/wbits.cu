@@ -176,10 +176,11 @@ void blst_p1s_mult_wbits(blst_p1* ret, const blst_p1_affine table[], size_t wbit
         if (gerr) return;
         void* dp = ctx->msm.points.get(npoints * sizeof(blst_p1_affine));
         void* ds = ctx->msm.scalars.get(npoints * nbytes + 16);
-        if (!dp || !ds) return;
-        // row heads: table[i * m], a strided copy
-        cudaError_t err = cudaMemcpy2DAsync(dp, sizeof(blst_p1_affine), table, m * sizeof(blst_p1_affine),
-                                            sizeof(blst_p1_affine), npoints, cudaMemcpyHostToDevice, st);
+        // row heads table[i * m] gathered into pinned staging: one dense copy
+        blst_p1_affine* heads = (blst_p1_affine*)ctx->h_points.get(npoints * sizeof(blst_p1_affine));
+        if (!dp || !ds || !heads) return;
+        for (size_t i = 0; i < npoints; i++) heads[i] = table[i * m];
+        cudaError_t err = cudaMemcpyAsync(dp, heads, npoints * sizeof(blst_p1_affine), cudaMemcpyHostToDevice, st);
         if (err == cudaSuccess) err = cudaMemcpyAsync(ds, hs, npoints * nbytes, cudaMemcpyHostToDevice, st);
         uint64_t out[18];
         if (err == cudaSuccess)

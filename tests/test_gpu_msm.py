@@ -47,6 +47,27 @@ def test_fp_mul_matches_oracle(gpu, oracle, synth):
         assert int.from_bytes(got[48 * i:48 * i + 48], "little") == exp, i
 
 
+def test_fp_sqr_matches_bigint(gpu):
+    """The dedicated squaring (catmsm_fp_mul with a == b) on lazily reduced
+    inputs in [0, 2p), including the boundary values."""
+    import random
+    rnd = random.Random(6)
+    p = 0x1a0111ea397fe69a4b1ba7b6434bacd764774b84f38512bf6730d2a0f6b0f6241eabfffeb153ffffb9feffffffffaaab
+    vals = [0, 1, 2, p - 1, p, p + 1, 2 * p - 1, 2 * p - 2, (p + 1) // 2, (1 << 381) - 1, (1 << 32) - 1,
+            sum(0xffffffff << (64 * k) for k in range(6)) % (2 * p)]
+    vals += [rnd.randrange(2 * p) for _ in range(4000)]
+    n = len(vals)
+    buf = b"".join(x.to_bytes(48, "little") for x in vals)
+    out = bytearray(48 * n)
+    import ctypes as C
+    L = gpu.load()
+    ab = (C.c_char * len(buf)).from_buffer(bytearray(buf))
+    assert L.catmsm_fp_mul((C.c_char * len(out)).from_buffer(out), ab, ab, n) == 0
+    rinv = pow(1 << 384, -1, p)
+    for i, x in enumerate(vals):
+        assert int.from_bytes(out[48 * i:48 * i + 48], "little") == x * x * rinv % p, i
+
+
 def test_points_from_scalars_matches_oracle(gpu, oracle, synth):
     n = 3000
     k = synth.point_scalars(77, n)
@@ -183,10 +204,12 @@ def test_msm_hot_buckets(gpu, oracle, synth):
     assert oracle.compress(gpu.p1s_mult_pippenger(pts, sc, n, 255)) == oracle.msm(pts, sc, n, 255)
 
 
+@pytest.mark.parametrize("glv", [0, 1])
 @pytest.mark.parametrize("window", [2, 5, 8, 13, 15, 16, 17, 20])
-def test_msm_device_windows(gpu, oracle, synth, window):
-    """Device-resident entry point over every window width class, including
-    widths where 255 is a multiple of c (a carry-only top window)."""
+def test_msm_device_windows(gpu, oracle, synth, window, glv):
+    """Device-resident entry point over every window width class, with and
+    without the GLV split; without it, 15 and 17 divide 255 (a carry-only
+    top window)."""
     import torch
     n = 20000
     pts = oracle.gen_points(40 + window, n)
@@ -194,5 +217,46 @@ def test_msm_device_windows(gpu, oracle, synth, window):
     dp = torch.frombuffer(bytearray(pts), dtype=torch.uint8).cuda()
     ds = torch.frombuffer(bytearray(sc), dtype=torch.uint8).cuda()
     torch.cuda.synchronize()
-    got = gpu.msm_device(dp.data_ptr(), ds.data_ptr(), 32, n, 255, window)
+    prev = gpu.msm_glv(glv)
+    try:
+        got = gpu.msm_device(dp.data_ptr(), ds.data_ptr(), 32, n, 255, window)
+    finally:
+        gpu.msm_glv(prev)
     assert oracle.compress(got) == oracle.msm(pts, sc, n, 255)
+
+
+LAMBDA = 0xac45a4010001a40200000000ffffffff
+
+
+def test_msm_glv_split_edge_scalars(gpu, oracle, synth):
+    """Scalars at the GLV split's boundaries (0, 1, lambda and its
+    neighbours, (lambda+1)/2, multiples of lambda, r - 1, r, r + 1, values
+    above 2r up to 2^256 - 1), infinity and repeated points: the GLV path
+    equals the plain path and the oracle, and the plan doubles the points."""
+    half = (LAMBDA + 1) // 2
+    ks = [0, 1, 2, LAMBDA - 1, LAMBDA, LAMBDA + 1, half - 1, half, half + 1, R - 1, R, R + 1, 2 * R + 5,
+          (1 << 256) - 1, (1 << 255), LAMBDA * LAMBDA, LAMBDA * LAMBDA + LAMBDA, half * LAMBDA,
+          (half - 1) * LAMBDA + half, (LAMBDA + 1) * LAMBDA - 1, R - LAMBDA, R - half]
+    ks += [int.from_bytes(synth.scalars(77, 1, 0), "little") + j * LAMBDA for j in range(10)]
+    n = len(ks)
+    pts = bytearray(oracle.gen_points(78, n))
+    pts[96 * 3:96 * 4] = bytes(96)                      # a point at infinity
+    pts[96 * 5:96 * 6] = pts[96 * 6:96 * 7]             # a repeated point
+    pts = bytes(pts)
+    sc = b"".join((k % (1 << 256)).to_bytes(32, "little") for k in ks)
+    assert gpu.msm_plan(n, 256)[2] == 2 * n and gpu.msm_plan(n, 128)[2] == n
+    exp = oracle.msm(pts, sc, n, 256)
+    assert oracle.compress(gpu.p1s_mult_pippenger(pts, sc, n, 256)) == exp
+    prev = gpu.msm_glv(0)
+    try:
+        assert gpu.msm_plan(n, 256)[2] == n
+        assert oracle.compress(gpu.p1s_mult_pippenger(pts, sc, n, 256)) == exp
+    finally:
+        gpu.msm_glv(prev)
+    # one point per scalar: every split alone
+    for i, k in enumerate(ks):
+        p1 = pts[96 * i:96 * i + 96]
+        s1 = sc[32 * i:32 * i + 32]
+        two = p1 + p1
+        got = gpu.p1s_mult_pippenger(two, s1 + bytes(32), 2, 256)
+        assert oracle.compress(got) == oracle.msm(two, s1 + bytes(32), 2, 256), hex(k)
