@@ -142,6 +142,33 @@ size_t blst_p1s_mult_wbits_scratch_sizeof(size_t npoints);
 void blst_p1s_mult_wbits(blst_p1 *ret, const blst_p1_affine table[], size_t wbits, size_t npoints,
                          const blst_byte *const scalars[], size_t nbits, blst_limb_t *scratch);
 
+/* Replaces blst_p1s_mult_fr_scratch_sizeof (bindings/blst_scalar.h:592,
+ * blst/c_api.cpp:1502-1506 -> :758-807): the reference policy MSM's capacity
+ * query, the larger of the Pippenger and the planned batch-affine sizes. */
+size_t blst_p1s_mult_fr_scratch_sizeof(size_t max_points);
+
+/* Replaces blst_p1s_mult_fr (bindings/blst_scalar.h:597, blst/c_api.cpp:
+ * 1508-1520 -> :809-850): same contract as blst_p1s_mult_pippenger_fr with
+ * the policy scratch size above. */
+bool blst_p1s_mult_fr(blst_p1 *ret, const blst_p1_affine points[], const blst_fr scalars[], size_t npoints,
+                      blst_limb_t *scratch, size_t scratch_size);
+
+/* Replaces blst_p1s_mult_batch_affine_fr_scratch_sizeof (bindings/blst_scalar.h:
+ * 599, blst/c_api.cpp:1522-1529 -> :593-639): 32 n + 256 * 2^(window-1) +
+ * 108 * batch_size (32 for n == 1); 0 for n == 0, n >= 2^32, window outside
+ * [1, 24] or batch_size not 128 or 384. */
+size_t blst_p1s_mult_batch_affine_fr_scratch_sizeof(size_t npoints, size_t window, size_t batch_size);
+
+/* Replaces blst_p1s_mult_batch_affine_fr (bindings/blst_scalar.h:601,
+ * blst/c_api.cpp:1531-1545 -> :641-690): NULL ret -> false; n == 0 ->
+ * infinity and true; an invalid window/batch size, NULL inputs or scratch
+ * below the queried size -> false with ret unchanged.  window and batch_size
+ * select the reference's CPU schedule; the GPU computes the same group
+ * element with its own. */
+bool blst_p1s_mult_batch_affine_fr(blst_p1 *ret, const blst_p1_affine points[], const blst_fr scalars[],
+                                   size_t npoints, blst_limb_t *scratch, size_t scratch_size, size_t window,
+                                   size_t batch_size);
+
 /* ------------------------------------------------------------------ Part 2 */
 
 /* MSM over DEVICE-resident inputs (no reference counterpart): d_points is n

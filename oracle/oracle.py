@@ -330,6 +330,14 @@ class Reference(_Common):
         L.blst_p1s_mult_pippenger_fr_scratch_sizeof.argtypes = [_sz]
         L.blst_p1s_mult_pippenger_fr.restype = C.c_bool
         L.blst_p1s_mult_pippenger_fr.argtypes = [_vp, _vp, _vp, _sz, _vp, _sz]
+        L.blst_p1s_mult_fr_scratch_sizeof.restype = _sz
+        L.blst_p1s_mult_fr_scratch_sizeof.argtypes = [_sz]
+        L.blst_p1s_mult_fr.restype = C.c_bool
+        L.blst_p1s_mult_fr.argtypes = [_vp, _vp, _vp, _sz, _vp, _sz]
+        L.blst_p1s_mult_batch_affine_fr_scratch_sizeof.restype = _sz
+        L.blst_p1s_mult_batch_affine_fr_scratch_sizeof.argtypes = [_sz, _sz, _sz]
+        L.blst_p1s_mult_batch_affine_fr.restype = C.c_bool
+        L.blst_p1s_mult_batch_affine_fr.argtypes = [_vp, _vp, _vp, _sz, _vp, _sz, _sz, _sz]
         self._msm = L.blst_p1s_mult_pippenger
         self.scratch_sizeof = L.blst_p1s_mult_pippenger_scratch_sizeof
         self._bind_wbits("blst_")
@@ -416,6 +424,23 @@ class Reference(_Common):
         ret = bytearray(P1)
         ok = self.L.blst_p1s_mult_pippenger_fr(_buf(ret), _buf(points), _buf(frs), n, scratch, sz)
         assert ok
+        return self.compress(bytes(ret))
+
+    def mult_fr(self, points: bytes, frs: bytes, n: int) -> bytes:
+        """blst_p1s_mult_fr (policy MSM) -> compressed."""
+        size = self.L.blst_p1s_mult_fr_scratch_sizeof(n)
+        scratch = (C.c_uint64 * (size // 8 + 1))()
+        ret = bytearray(P1)
+        assert self.L.blst_p1s_mult_fr(_buf(ret), _buf(bytearray(points)), _buf(bytearray(frs)), n, scratch, size)
+        return self.compress(bytes(ret))
+
+    def batch_affine_fr(self, points: bytes, frs: bytes, n: int, window: int, batch: int) -> bytes:
+        """blst_p1s_mult_batch_affine_fr -> compressed."""
+        size = self.L.blst_p1s_mult_batch_affine_fr_scratch_sizeof(n, window, batch)
+        scratch = (C.c_uint64 * (size // 8 + 1))()
+        ret = bytearray(P1)
+        assert self.L.blst_p1s_mult_batch_affine_fr(_buf(ret), _buf(bytearray(points)), _buf(bytearray(frs)), n,
+                                                    scratch, size, window, batch)
         return self.compress(bytes(ret))
 
 

@@ -129,6 +129,14 @@ def load(build_if_missing=True):
     L.catmsm_profile_entries.argtypes = []
     L.catmsm_profile_read.restype = C.c_int
     L.catmsm_profile_read.argtypes = [_vp, C.c_int, _vp]
+    L.blst_p1s_mult_fr_scratch_sizeof.restype = _sz
+    L.blst_p1s_mult_fr_scratch_sizeof.argtypes = [_sz]
+    L.blst_p1s_mult_fr.restype = C.c_bool
+    L.blst_p1s_mult_fr.argtypes = [_vp, _vp, _vp, _sz, _vp, _sz]
+    L.blst_p1s_mult_batch_affine_fr_scratch_sizeof.restype = _sz
+    L.blst_p1s_mult_batch_affine_fr_scratch_sizeof.argtypes = [_sz, _sz, _sz]
+    L.blst_p1s_mult_batch_affine_fr.restype = C.c_bool
+    L.blst_p1s_mult_batch_affine_fr.argtypes = [_vp, _vp, _vp, _sz, _vp, _sz, _sz, _sz]
     L.blst_p1s_mult_wbits_precompute_sizeof.restype = _sz
     L.blst_p1s_mult_wbits_precompute_sizeof.argtypes = [_sz, _sz]
     L.blst_p1s_mult_wbits_precompute.restype = None
@@ -274,6 +282,39 @@ def p1s_mult_pippenger_fr(points: bytes, frs: bytes, n: int, scratch_size=None, 
 
 def p1s_mult_pippenger_fr_scratch_sizeof(n: int) -> int:
     return load().blst_p1s_mult_pippenger_fr_scratch_sizeof(n)
+
+
+def p1s_mult_fr(points: bytes, frs: bytes, n: int, scratch_size=None, ret_init=None):
+    """blst_p1s_mult_fr; returns (ok, 144-byte ret)."""
+    L = load()
+    size = L.blst_p1s_mult_fr_scratch_sizeof(n) if scratch_size is None else scratch_size
+    scratch = (C.c_uint64 * (max(size, 8) // 8 + 1))() if size >= 0 else None
+    ret = bytearray(ret_init if ret_init is not None else bytes(P1))
+    ok = L.blst_p1s_mult_fr(_buf(ret), _buf(bytearray(points)) if points else None,
+                            _buf(bytearray(frs)) if frs else None, n, scratch, size if size >= 0 else 0)
+    return ok, bytes(ret)
+
+
+def p1s_mult_fr_scratch_sizeof(n: int) -> int:
+    return load().blst_p1s_mult_fr_scratch_sizeof(n)
+
+
+def p1s_mult_batch_affine_fr(points: bytes, frs: bytes, n: int, window: int, batch_size: int,
+                             scratch_size=None, ret_init=None):
+    """blst_p1s_mult_batch_affine_fr; returns (ok, 144-byte ret)."""
+    L = load()
+    need = L.blst_p1s_mult_batch_affine_fr_scratch_sizeof(n, window, batch_size)
+    size = need if scratch_size is None else scratch_size
+    scratch = (C.c_uint64 * (max(size, 8) // 8 + 1))() if size >= 0 else None
+    ret = bytearray(ret_init if ret_init is not None else bytes(P1))
+    ok = L.blst_p1s_mult_batch_affine_fr(_buf(ret), _buf(bytearray(points)) if points else None,
+                                         _buf(bytearray(frs)) if frs else None, n, scratch,
+                                         size if size >= 0 else 0, window, batch_size)
+    return ok, bytes(ret)
+
+
+def p1s_mult_batch_affine_fr_scratch_sizeof(n: int, window: int, batch_size: int) -> int:
+    return load().blst_p1s_mult_batch_affine_fr_scratch_sizeof(n, window, batch_size)
 
 
 def fr_fft(values: bytes, n: int, inverse: bool):

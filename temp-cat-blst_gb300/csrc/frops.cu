@@ -1,8 +1,13 @@
 // Scalar-field (Fr) entry points on sm_103a:
 //  * blst_p1s_mult_pippenger_fr (reference blst/c_api.cpp:1420-1435 ->
-//    c_api_pippenger_fr :532-585): Montgomery-form blst_fr scalars are
+//    c_api_pippenger_fr :532-585), blst_p1s_mult_fr (:1502-1520 ->
+//    c_api_msm_fr :809-850) and blst_p1s_mult_batch_affine_fr (:1522-1545 ->
+//    c_api_batch_affine_fr :641-690): Montgomery-form blst_fr scalars are
 //    converted to canonical integers on the device (Fr::to_scaler, i.e.
-//    from_mont), then the G1 MSM pipeline runs with nbits = 255;
+//    from_mont), then the G1 MSM pipeline runs with nbits = 255.  The three
+//    differ only in their scratch contracts, which are kept exactly (the
+//    reference's batch-affine algorithm and window are a CPU schedule; the
+//    result is the same group element);
 //  * blst_fr_fft / blst_fr_fft_with_domain (reference blst/fft_c_api.cpp:
 //    109-182): radix-2 DIT over Fr with the reference's schedule and root
 //    indexing (ctFft.h:50-94; FrCoeffCtx plus/minus/mult = Fr add/sub/mul).
@@ -16,6 +21,7 @@
 #include "host_fr.hpp"
 #include "catmsm_gpu.h"
 
+#include <algorithm>
 #include <climits>
 #include <cstring>
 
@@ -222,6 +228,89 @@ static size_t pippenger_fr_scratch(size_t n)
     return scalar_bytes + buckets * 192;
 }
 
+// reference c_api_batch_affine_fr_scratch_sizeof (c_api.cpp:593-639) with
+// msm_mult_batch_affine_scratch_sizeof (multi_scalar_batch_affine.cpp:149-170,
+// :468-471): 32 n canonical-scalar bytes plus, for n > 1, 2^(w-1) 256-byte
+// bucket pairs and 108 bytes per batch slot; B in {128, 384}, w in [1, 24],
+// n < 2^32.
+static size_t batch_affine_fr_scratch(size_t n, size_t w, size_t B)
+{
+    if (n == 0 || n > 0xffffffffull) return 0;
+    if ((B != 128 && B != 384) || w < 1 || w > 24) return 0;
+    const size_t alg = ((size_t)256 << (w - 1)) + 108 * B;
+    if (n > SIZE_MAX / 32) return 0;
+    const size_t scalar_bytes = n * 32;
+    if (n == 1) return scalar_bytes;
+    if (alg > SIZE_MAX - scalar_bytes) return 0;
+    return scalar_bytes + alg;
+}
+
+// reference c_api_msm_fr_plan (c_api.cpp:723-756): the window and batch size
+// the reference's policy MSM picks (window 0 = Pippenger).
+static void msm_fr_plan(size_t n, size_t* w, size_t* B)
+{
+    *w = 0;
+    *B = 0;
+    if (n < ((size_t)1 << 12) || n > ((size_t)1 << 18)) return;
+    if (n <= ((size_t)1 << 12)) *w = 10;
+    else if (n <= ((size_t)1 << 14)) *w = 11;
+    else if (n <= ((size_t)1 << 15)) *w = 12;
+    else if (n <= ((size_t)1 << 16)) *w = 13;
+    else if (n <= ((size_t)1 << 17)) *w = 14;
+    else *w = 15;
+    *B = n >= ((size_t)1 << 18) ? 384 : 128;
+}
+
+// reference c_api_msm_fr_scratch_sizeof (c_api.cpp:758-807): a capacity
+// query, the larger of the Pippenger and the planned batch-affine sizes (and
+// of the largest measured batch plan above 2^18 points).
+static size_t mult_fr_scratch(size_t n)
+{
+    if (n == 0) return 0;
+    size_t req = pippenger_fr_scratch(n);
+    if (req == 0) return 0;
+    size_t w, B;
+    msm_fr_plan(n, &w, &B);
+    if (w) {
+        const size_t b = batch_affine_fr_scratch(n, w, B);
+        if (b == 0) return 0;
+        req = std::max(req, b);
+    }
+    const size_t measured = (size_t)1 << 18;
+    if (n > measured) {
+        msm_fr_plan(measured, &w, &B);
+        const size_t b = batch_affine_fr_scratch(measured, w, B);
+        if (b == 0) return 0;
+        req = std::max(req, b);
+    }
+    return req;
+}
+
+// Montgomery-form scalars -> canonical integers on the device, then the MSM
+// pipeline over 255-bit scalars; ret untouched unless it succeeds.
+static bool fr_msm_run(blst_p1* ret, const blst_p1_affine points[], const blst_fr scalars[], size_t npoints)
+{
+    if (npoints > 0x7fffffffu) return false;
+    Ctx* ctx = get_ctx();
+    if (!ctx) return false;
+    void* dp = ctx->msm.points.get(npoints * sizeof(blst_p1_affine));
+    uint32_t* ds = (uint32_t*)ctx->msm.scalars.get(npoints * 32 + 16);
+    if (!dp || !ds) return false;
+    cudaStream_t st = ctx->stream;
+    cudaError_t err = cudaMemcpyAsync(dp, points, npoints * sizeof(blst_p1_affine), cudaMemcpyHostToDevice, st);
+    if (err == cudaSuccess) err = cudaMemcpyAsync(ds, scalars, npoints * 32, cudaMemcpyHostToDevice, st);
+    if (err == cudaSuccess) {
+        k_fr_to_canonical<<<div_up(npoints, 256), 256, 0, st>>>(ds, (uint32_t)npoints);
+        g_stats.launches++;
+        err = cudaGetLastError();
+    }
+    uint64_t out[18];
+    if (err == cudaSuccess) err = msm_device(ctx, dp, (const uint8_t*)ds, 32, npoints, 255, 0, out);
+    if (err != cudaSuccess) return false;
+    std::memcpy(ret, out, sizeof(*ret));
+    return true;
+}
+
 }  // namespace catmsm
 
 using namespace catmsm;
@@ -241,25 +330,49 @@ bool blst_p1s_mult_pippenger_fr(blst_p1* ret, const blst_p1_affine points[], con
         }
         const size_t required = pippenger_fr_scratch(npoints);
         if (required == 0 || !points || !scalars || !scratch || scratch_size < required) return false;
-        if (npoints > 0x7fffffffu) return false;
-        Ctx* ctx = get_ctx();
-        if (!ctx) return false;
-        void* dp = ctx->msm.points.get(npoints * sizeof(blst_p1_affine));
-        uint32_t* ds = (uint32_t*)ctx->msm.scalars.get(npoints * 32 + 16);
-        if (!dp || !ds) return false;
-        cudaStream_t st = ctx->stream;
-        cudaError_t err = cudaMemcpyAsync(dp, points, npoints * sizeof(blst_p1_affine), cudaMemcpyHostToDevice, st);
-        if (err == cudaSuccess) err = cudaMemcpyAsync(ds, scalars, npoints * 32, cudaMemcpyHostToDevice, st);
-        if (err == cudaSuccess) {
-            k_fr_to_canonical<<<div_up(npoints, 256), 256, 0, st>>>(ds, (uint32_t)npoints);
-            g_stats.launches++;
-            err = cudaGetLastError();
+        return fr_msm_run(ret, points, scalars, npoints);
+    } catch (...) {
+        return false;
+    }
+}
+
+size_t blst_p1s_mult_fr_scratch_sizeof(size_t max_points) { return mult_fr_scratch(max_points); }
+
+bool blst_p1s_mult_fr(blst_p1* ret, const blst_p1_affine points[], const blst_fr scalars[], size_t npoints,
+                      blst_limb_t* scratch, size_t scratch_size)
+{
+    try {
+        if (!ret) return false;
+        if (npoints == 0) {
+            std::memset(ret, 0, sizeof(*ret));
+            return true;
         }
-        uint64_t out[18];
-        if (err == cudaSuccess) err = msm_device(ctx, dp, (const uint8_t*)ds, 32, npoints, 255, 0, out);
-        if (err != cudaSuccess) return false;
-        std::memcpy(ret, out, sizeof(*ret));
-        return true;
+        const size_t required = mult_fr_scratch(npoints);
+        if (required == 0 || !points || !scalars || !scratch || scratch_size < required) return false;
+        return fr_msm_run(ret, points, scalars, npoints);
+    } catch (...) {
+        return false;
+    }
+}
+
+size_t blst_p1s_mult_batch_affine_fr_scratch_sizeof(size_t npoints, size_t window, size_t batch_size)
+{
+    return batch_affine_fr_scratch(npoints, window, batch_size);
+}
+
+bool blst_p1s_mult_batch_affine_fr(blst_p1* ret, const blst_p1_affine points[], const blst_fr scalars[],
+                                   size_t npoints, blst_limb_t* scratch, size_t scratch_size, size_t window,
+                                   size_t batch_size)
+{
+    try {
+        if (!ret) return false;
+        if (npoints == 0) {
+            std::memset(ret, 0, sizeof(*ret));
+            return true;
+        }
+        const size_t required = batch_affine_fr_scratch(npoints, window, batch_size);
+        if (required == 0 || !points || !scalars || !scratch || scratch_size < required) return false;
+        return fr_msm_run(ret, points, scalars, npoints);
     } catch (...) {
         return false;
     }

@@ -15,7 +15,11 @@ reference's own C ABI built from its sources (oracle/_ref/libblst_ref.so):
   * wbits:  blst_p1s_mult_wbits_precompute table bytes (sha256) and
             blst_p1s_mult_wbits -> compressed, per (n, wbits, nbits)
 
-`--section wbits` regenerates only that section of an existing file.
+  * msm_fr_variants: blst_p1s_mult_fr and blst_p1s_mult_batch_affine_fr ->
+            compressed, and the reference's scratch-size queries for both
+
+`--section wbits|msm_fr_variants` regenerates only that section of an
+existing file.
 """
 import hashlib
 import json
@@ -75,13 +79,47 @@ def wbits_section(o, r):
     return out
 
 
+FR_VARIANT_CASES = [
+    # (api, seed, n, window, batch, inf)
+    ("mult_fr", 81, 1, 0, 0, False), ("mult_fr", 82, 2, 0, 0, False), ("mult_fr", 83, 100, 0, 0, True),
+    ("mult_fr", 84, 4096, 0, 0, False), ("mult_fr", 85, 5000, 0, 0, False), ("mult_fr", 86, 4096, 0, 0, True),
+    ("mult_fr", 87, 1 << 15, 0, 0, False),
+    ("batch_affine_fr", 91, 1, 5, 128, False), ("batch_affine_fr", 92, 2, 1, 128, False),
+    ("batch_affine_fr", 93, 100, 5, 384, False), ("batch_affine_fr", 94, 1000, 10, 128, False),
+    ("batch_affine_fr", 95, 4096, 13, 384, False),
+]
+
+
+def fr_variants_section(o, r):
+    out = {"cases": [], "mult_fr_scratch": [], "batch_affine_scratch": []}
+    for api, seed, n, w, b, inf in FR_VARIANT_CASES:
+        pts = o.gen_points(seed, n)
+        if inf:
+            k = seed % n
+            pts = pts[:96 * k] + bytes(96) + pts[96 * (k + 1):]
+        frs = b"".join(o.fr_to_mont(o.gen_scalars(seed + 1000, n, 0)[32 * i:32 * i + 32]) for i in range(n))
+        res = r.mult_fr(pts, frs, n) if api == "mult_fr" else r.batch_affine_fr(pts, frs, n, w, b)
+        out["cases"].append({"api": api, "seed": seed, "n": n, "window": w, "batch": b, "inf": inf,
+                             "compressed": res.hex()})
+        print(api, seed, n, w, b, res.hex()[:16], flush=True)
+    for n in (0, 1, 2, 100, 4095, 4096, 4097, 1 << 14, (1 << 14) + 1, 1 << 15, 1 << 16, 1 << 17, 1 << 18,
+              (1 << 18) + 1, 1 << 20, 1 << 22):
+        out["mult_fr_scratch"].append([n, r.L.blst_p1s_mult_fr_scratch_sizeof(n)])
+    for n in (0, 1, 2, 3, 1000, (1 << 32) - 1, 1 << 32):
+        for w in (0, 1, 2, 10, 24, 25):
+            for b in (0, 100, 128, 384, 512):
+                out["batch_affine_scratch"].append([n, w, b, r.L.blst_p1s_mult_batch_affine_fr_scratch_sizeof(n, w, b)])
+    return out
+
+
 def main():
     large = "--large" in sys.argv
     build(ref=True)
     o, r = Oracle(), Reference()
-    if "--section" in sys.argv and sys.argv[sys.argv.index("--section") + 1] == "wbits":
+    if "--section" in sys.argv:
+        name = sys.argv[sys.argv.index("--section") + 1]
         g = json.load(open(OUT))
-        g["wbits"] = wbits_section(o, r)
+        g[name] = {"wbits": wbits_section, "msm_fr_variants": fr_variants_section}[name](o, r)
         json.dump(g, open(OUT, "w"), indent=1)
         print("wrote", OUT)
         return
@@ -162,6 +200,7 @@ def main():
             g["fr_fft"].append({"seed": seed, "n": n, "mode": mode, "sha256": hashlib.sha256(out).hexdigest()})
         print("fr_fft", seed, n, flush=True)
     g["wbits"] = wbits_section(o, r)
+    g["msm_fr_variants"] = fr_variants_section(o, r)
     if not large and os.path.exists(OUT):
         # keep previously generated large cases
         old = json.load(open(OUT))

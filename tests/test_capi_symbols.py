@@ -60,3 +60,12 @@ def test_wbits_sizes_match_reference_contract(gpu_binding, oracle):
     assert gpu_binding.p1s_mult_wbits_precompute_sizeof(15, 10) == 0
     for n in (0, 1, 4096, 8191, 8192, 8193, 1 << 20):
         assert gpu_binding.p1s_mult_wbits_scratch_sizeof(n) == oracle.wbits_scratch_sizeof(n) == 144 * min(n, 8192)
+
+
+def test_fr_msm_variant_sizes_match_reference(gpu_binding, golden):
+    # pure host functions: no device call; values recorded from the reference
+    g = golden["msm_fr_variants"]
+    for n, exp in g["mult_fr_scratch"]:
+        assert gpu_binding.p1s_mult_fr_scratch_sizeof(n) == exp, n
+    for n, w, b, exp in g["batch_affine_scratch"]:
+        assert gpu_binding.p1s_mult_batch_affine_fr_scratch_sizeof(n, w, b) == exp, (n, w, b)

@@ -240,3 +240,18 @@ def test_oracle_wbits_matches_reference_edge_cases(oracle):
         oracle.L.oracle_p1s_mult_wbits((C.c_char * 144).from_buffer(r1), tb2, args[0], n, sarr, args[1], args[2])
         ref.L.blst_p1s_mult_wbits((C.c_char * 144).from_buffer(r2), tb2, args[0], n, sarr, args[1], args[2])
         assert oracle.compress(bytes(r1)) == ref.compress(bytes(r2)) == inf
+
+
+def test_oracle_matches_fr_msm_variant_goldens(golden, oracle):
+    """blst_p1s_mult_fr / blst_p1s_mult_batch_affine_fr outputs of the
+    reference equal the oracle's MSM of the same Montgomery scalars."""
+    for c in golden["msm_fr_variants"]["cases"]:
+        n = c["n"]
+        if n > 5000:
+            continue
+        pts = oracle.gen_points(c["seed"], n)
+        if c["inf"]:
+            k = c["seed"] % n
+            pts = pts[:96 * k] + bytes(96) + pts[96 * (k + 1):]
+        frs = _frs(oracle, c["seed"] + 1000, n)
+        assert oracle.msm_fr(pts, frs, n).hex() == c["compressed"], (c["api"], n)
