@@ -174,7 +174,962 @@ static __device__ __noinline__ fp fp_mul_call(const fp a, const fp b)
 
 __device__ __forceinline__ void fp_mul(fp& r, const fp& a, const fp& b) { r = fp_mul_call(a, b); }
 
-__device__ __forceinline__ void fp_sqr(fp& r, const fp& a) { fp_mul(r, a, a); }
+// r = a^2 * 2^-384 mod p; input in [0, 2p), output in [0, 2p).  The CIOS
+// schedule of fp_mul_impl with the symmetry of a square: step i adds
+// a_i * V_i, V_i = a_i 2^(32i) + 2 sum_{j>i} a_j 2^(32j) (a < 2p keeps the top word
+// below 2^30, so doubling stays in 12 words), i.e. 12 - i limb products
+// instead of 12: 156 product IMAD instead of 288.  Products of even and odd
+// positions go to the independent E and O accumulators as in fp_mul_impl, and
+// the Montgomery step is the same.  Each step adds at most 4p 2^32, so the
+// running value stays below 6p < 2^384 and the result below 2p.
+__device__ __forceinline__ void fp_sqr_impl(fp& r, const fp& a)
+{
+    uint32_t t[12], e[13], o[13], d[12];
+#pragma unroll
+    for (int j = 1; j < 12; j++) d[j] = __funnelshift_l(a.v[j - 1], a.v[j], 1);   // (2a)_j
+    {   // step 0
+        const uint32_t bi = a.v[0];
+#pragma unroll
+        for (int k = 0; k < 13; k++) e[k] = 0;
+        e[0] = a.v[0] * bi;
+        e[1] = __umulhi(a.v[0], bi);
+        e[2] = d[2] * bi;
+        e[3] = __umulhi(d[2], bi);
+        e[4] = d[4] * bi;
+        e[5] = __umulhi(d[4], bi);
+        e[6] = d[6] * bi;
+        e[7] = __umulhi(d[6], bi);
+        e[8] = d[8] * bi;
+        e[9] = __umulhi(d[8], bi);
+        e[10] = d[10] * bi;
+        e[11] = __umulhi(d[10], bi);
+#pragma unroll
+        for (int k = 0; k < 13; k++) o[k] = 0;
+        o[0] = (a.v[1] << 1) * bi;
+        o[1] = __umulhi((a.v[1] << 1), bi);
+        o[2] = d[3] * bi;
+        o[3] = __umulhi(d[3], bi);
+        o[4] = d[5] * bi;
+        o[5] = __umulhi(d[5], bi);
+        o[6] = d[7] * bi;
+        o[7] = __umulhi(d[7], bi);
+        o[8] = d[9] * bi;
+        o[9] = __umulhi(d[9], bi);
+        o[10] = d[11] * bi;
+        o[11] = __umulhi(d[11], bi);
+        const uint32_t m = e[0] * CATMSM_N0;
+        asm("mad.lo.cc.u32  %0, %13, %14, %0;\n\t"
+            "madc.hi.cc.u32 %1, %13, %14, %1;\n\t"
+            "madc.lo.cc.u32 %2, %13, %15, %2;\n\t"
+            "madc.hi.cc.u32 %3, %13, %15, %3;\n\t"
+            "madc.lo.cc.u32 %4, %13, %16, %4;\n\t"
+            "madc.hi.cc.u32 %5, %13, %16, %5;\n\t"
+            "madc.lo.cc.u32 %6, %13, %17, %6;\n\t"
+            "madc.hi.cc.u32 %7, %13, %17, %7;\n\t"
+            "madc.lo.cc.u32 %8, %13, %18, %8;\n\t"
+            "madc.hi.cc.u32 %9, %13, %18, %9;\n\t"
+            "madc.lo.cc.u32 %10, %13, %19, %10;\n\t"
+            "madc.hi.cc.u32 %11, %13, %19, %11;\n\t"
+            "addc.u32       %12, %12, 0;"
+            : "+r"(e[0]), "+r"(e[1]), "+r"(e[2]), "+r"(e[3]), "+r"(e[4]), "+r"(e[5]),
+              "+r"(e[6]), "+r"(e[7]), "+r"(e[8]), "+r"(e[9]), "+r"(e[10]), "+r"(e[11]),
+              "+r"(e[12])
+            : "r"(m), "n"(CATMSM_P0), "n"(CATMSM_P2), "n"(CATMSM_P4), "n"(CATMSM_P6),
+              "n"(CATMSM_P8), "n"(CATMSM_P10));
+        asm("mad.lo.cc.u32  %0, %13, %14, %0;\n\t"
+            "madc.hi.cc.u32 %1, %13, %14, %1;\n\t"
+            "madc.lo.cc.u32 %2, %13, %15, %2;\n\t"
+            "madc.hi.cc.u32 %3, %13, %15, %3;\n\t"
+            "madc.lo.cc.u32 %4, %13, %16, %4;\n\t"
+            "madc.hi.cc.u32 %5, %13, %16, %5;\n\t"
+            "madc.lo.cc.u32 %6, %13, %17, %6;\n\t"
+            "madc.hi.cc.u32 %7, %13, %17, %7;\n\t"
+            "madc.lo.cc.u32 %8, %13, %18, %8;\n\t"
+            "madc.hi.cc.u32 %9, %13, %18, %9;\n\t"
+            "madc.lo.cc.u32 %10, %13, %19, %10;\n\t"
+            "madc.hi.cc.u32 %11, %13, %19, %11;\n\t"
+            "addc.u32       %12, 0, 0;"
+            : "+r"(o[0]), "+r"(o[1]), "+r"(o[2]), "+r"(o[3]), "+r"(o[4]), "+r"(o[5]),
+              "+r"(o[6]), "+r"(o[7]), "+r"(o[8]), "+r"(o[9]), "+r"(o[10]), "+r"(o[11]),
+              "=r"(o[12])
+            : "r"(m), "n"(CATMSM_P1), "n"(CATMSM_P3), "n"(CATMSM_P5), "n"(CATMSM_P7),
+              "n"(CATMSM_P9), "n"(CATMSM_P11));
+        asm("add.cc.u32  %0, %0, %12;\n\t"
+            "addc.cc.u32 %1, %1, %13;\n\t"
+            "addc.cc.u32 %2, %2, %14;\n\t"
+            "addc.cc.u32 %3, %3, %15;\n\t"
+            "addc.cc.u32 %4, %4, %16;\n\t"
+            "addc.cc.u32 %5, %5, %17;\n\t"
+            "addc.cc.u32 %6, %6, %18;\n\t"
+            "addc.cc.u32 %7, %7, %19;\n\t"
+            "addc.cc.u32 %8, %8, %20;\n\t"
+            "addc.cc.u32 %9, %9, %21;\n\t"
+            "addc.cc.u32 %10, %10, %22;\n\t"
+            "addc.u32    %11, %11, %23;"
+            : "+r"(o[0]), "+r"(o[1]), "+r"(o[2]), "+r"(o[3]), "+r"(o[4]), "+r"(o[5]),
+              "+r"(o[6]), "+r"(o[7]), "+r"(o[8]), "+r"(o[9]), "+r"(o[10]), "+r"(o[11])
+            : "r"(e[1]), "r"(e[2]), "r"(e[3]), "r"(e[4]), "r"(e[5]), "r"(e[6]),
+              "r"(e[7]), "r"(e[8]), "r"(e[9]), "r"(e[10]), "r"(e[11]), "r"(e[12]));
+#pragma unroll
+        for (int k = 0; k < 12; k++) t[k] = o[k];
+    }
+    {   // step 1
+        const uint32_t bi = a.v[1];
+#pragma unroll
+        for (int k = 0; k < 12; k++) e[k] = t[k];
+        asm("mad.lo.cc.u32  %0, %11, %16, %0;\n\t"
+            "madc.hi.cc.u32 %1, %11, %16, %1;\n\t"
+            "madc.lo.cc.u32 %2, %12, %16, %2;\n\t"
+            "madc.hi.cc.u32 %3, %12, %16, %3;\n\t"
+            "madc.lo.cc.u32 %4, %13, %16, %4;\n\t"
+            "madc.hi.cc.u32 %5, %13, %16, %5;\n\t"
+            "madc.lo.cc.u32 %6, %14, %16, %6;\n\t"
+            "madc.hi.cc.u32 %7, %14, %16, %7;\n\t"
+            "madc.lo.cc.u32 %8, %15, %16, %8;\n\t"
+            "madc.hi.cc.u32 %9, %15, %16, %9;\n\t"
+            "addc.u32       %10, 0, 0;"
+            : "+r"(e[2]), "+r"(e[3]), "+r"(e[4]), "+r"(e[5]), "+r"(e[6]), "+r"(e[7]), "+r"(e[8]), "+r"(e[9]), "+r"(e[10]), "+r"(e[11]), "=r"(e[12])
+            : "r"((a.v[2] << 1)), "r"(d[4]), "r"(d[6]), "r"(d[8]), "r"(d[10]), "r"(bi));
+#pragma unroll
+        for (int k = 0; k < 13; k++) o[k] = 0;
+        o[0] = a.v[1] * bi;
+        o[1] = __umulhi(a.v[1], bi);
+        o[2] = d[3] * bi;
+        o[3] = __umulhi(d[3], bi);
+        o[4] = d[5] * bi;
+        o[5] = __umulhi(d[5], bi);
+        o[6] = d[7] * bi;
+        o[7] = __umulhi(d[7], bi);
+        o[8] = d[9] * bi;
+        o[9] = __umulhi(d[9], bi);
+        o[10] = d[11] * bi;
+        o[11] = __umulhi(d[11], bi);
+        const uint32_t m = e[0] * CATMSM_N0;
+        asm("mad.lo.cc.u32  %0, %13, %14, %0;\n\t"
+            "madc.hi.cc.u32 %1, %13, %14, %1;\n\t"
+            "madc.lo.cc.u32 %2, %13, %15, %2;\n\t"
+            "madc.hi.cc.u32 %3, %13, %15, %3;\n\t"
+            "madc.lo.cc.u32 %4, %13, %16, %4;\n\t"
+            "madc.hi.cc.u32 %5, %13, %16, %5;\n\t"
+            "madc.lo.cc.u32 %6, %13, %17, %6;\n\t"
+            "madc.hi.cc.u32 %7, %13, %17, %7;\n\t"
+            "madc.lo.cc.u32 %8, %13, %18, %8;\n\t"
+            "madc.hi.cc.u32 %9, %13, %18, %9;\n\t"
+            "madc.lo.cc.u32 %10, %13, %19, %10;\n\t"
+            "madc.hi.cc.u32 %11, %13, %19, %11;\n\t"
+            "addc.u32       %12, %12, 0;"
+            : "+r"(e[0]), "+r"(e[1]), "+r"(e[2]), "+r"(e[3]), "+r"(e[4]), "+r"(e[5]),
+              "+r"(e[6]), "+r"(e[7]), "+r"(e[8]), "+r"(e[9]), "+r"(e[10]), "+r"(e[11]),
+              "+r"(e[12])
+            : "r"(m), "n"(CATMSM_P0), "n"(CATMSM_P2), "n"(CATMSM_P4), "n"(CATMSM_P6),
+              "n"(CATMSM_P8), "n"(CATMSM_P10));
+        asm("mad.lo.cc.u32  %0, %13, %14, %0;\n\t"
+            "madc.hi.cc.u32 %1, %13, %14, %1;\n\t"
+            "madc.lo.cc.u32 %2, %13, %15, %2;\n\t"
+            "madc.hi.cc.u32 %3, %13, %15, %3;\n\t"
+            "madc.lo.cc.u32 %4, %13, %16, %4;\n\t"
+            "madc.hi.cc.u32 %5, %13, %16, %5;\n\t"
+            "madc.lo.cc.u32 %6, %13, %17, %6;\n\t"
+            "madc.hi.cc.u32 %7, %13, %17, %7;\n\t"
+            "madc.lo.cc.u32 %8, %13, %18, %8;\n\t"
+            "madc.hi.cc.u32 %9, %13, %18, %9;\n\t"
+            "madc.lo.cc.u32 %10, %13, %19, %10;\n\t"
+            "madc.hi.cc.u32 %11, %13, %19, %11;\n\t"
+            "addc.u32       %12, 0, 0;"
+            : "+r"(o[0]), "+r"(o[1]), "+r"(o[2]), "+r"(o[3]), "+r"(o[4]), "+r"(o[5]),
+              "+r"(o[6]), "+r"(o[7]), "+r"(o[8]), "+r"(o[9]), "+r"(o[10]), "+r"(o[11]),
+              "=r"(o[12])
+            : "r"(m), "n"(CATMSM_P1), "n"(CATMSM_P3), "n"(CATMSM_P5), "n"(CATMSM_P7),
+              "n"(CATMSM_P9), "n"(CATMSM_P11));
+        asm("add.cc.u32  %0, %0, %12;\n\t"
+            "addc.cc.u32 %1, %1, %13;\n\t"
+            "addc.cc.u32 %2, %2, %14;\n\t"
+            "addc.cc.u32 %3, %3, %15;\n\t"
+            "addc.cc.u32 %4, %4, %16;\n\t"
+            "addc.cc.u32 %5, %5, %17;\n\t"
+            "addc.cc.u32 %6, %6, %18;\n\t"
+            "addc.cc.u32 %7, %7, %19;\n\t"
+            "addc.cc.u32 %8, %8, %20;\n\t"
+            "addc.cc.u32 %9, %9, %21;\n\t"
+            "addc.cc.u32 %10, %10, %22;\n\t"
+            "addc.u32    %11, %11, %23;"
+            : "+r"(o[0]), "+r"(o[1]), "+r"(o[2]), "+r"(o[3]), "+r"(o[4]), "+r"(o[5]),
+              "+r"(o[6]), "+r"(o[7]), "+r"(o[8]), "+r"(o[9]), "+r"(o[10]), "+r"(o[11])
+            : "r"(e[1]), "r"(e[2]), "r"(e[3]), "r"(e[4]), "r"(e[5]), "r"(e[6]),
+              "r"(e[7]), "r"(e[8]), "r"(e[9]), "r"(e[10]), "r"(e[11]), "r"(e[12]));
+#pragma unroll
+        for (int k = 0; k < 12; k++) t[k] = o[k];
+    }
+    {   // step 2
+        const uint32_t bi = a.v[2];
+#pragma unroll
+        for (int k = 0; k < 12; k++) e[k] = t[k];
+        asm("mad.lo.cc.u32  %0, %11, %16, %0;\n\t"
+            "madc.hi.cc.u32 %1, %11, %16, %1;\n\t"
+            "madc.lo.cc.u32 %2, %12, %16, %2;\n\t"
+            "madc.hi.cc.u32 %3, %12, %16, %3;\n\t"
+            "madc.lo.cc.u32 %4, %13, %16, %4;\n\t"
+            "madc.hi.cc.u32 %5, %13, %16, %5;\n\t"
+            "madc.lo.cc.u32 %6, %14, %16, %6;\n\t"
+            "madc.hi.cc.u32 %7, %14, %16, %7;\n\t"
+            "madc.lo.cc.u32 %8, %15, %16, %8;\n\t"
+            "madc.hi.cc.u32 %9, %15, %16, %9;\n\t"
+            "addc.u32       %10, 0, 0;"
+            : "+r"(e[2]), "+r"(e[3]), "+r"(e[4]), "+r"(e[5]), "+r"(e[6]), "+r"(e[7]), "+r"(e[8]), "+r"(e[9]), "+r"(e[10]), "+r"(e[11]), "=r"(e[12])
+            : "r"(a.v[2]), "r"(d[4]), "r"(d[6]), "r"(d[8]), "r"(d[10]), "r"(bi));
+#pragma unroll
+        for (int k = 0; k < 13; k++) o[k] = 0;
+        o[2] = (a.v[3] << 1) * bi;
+        o[3] = __umulhi((a.v[3] << 1), bi);
+        o[4] = d[5] * bi;
+        o[5] = __umulhi(d[5], bi);
+        o[6] = d[7] * bi;
+        o[7] = __umulhi(d[7], bi);
+        o[8] = d[9] * bi;
+        o[9] = __umulhi(d[9], bi);
+        o[10] = d[11] * bi;
+        o[11] = __umulhi(d[11], bi);
+        const uint32_t m = e[0] * CATMSM_N0;
+        asm("mad.lo.cc.u32  %0, %13, %14, %0;\n\t"
+            "madc.hi.cc.u32 %1, %13, %14, %1;\n\t"
+            "madc.lo.cc.u32 %2, %13, %15, %2;\n\t"
+            "madc.hi.cc.u32 %3, %13, %15, %3;\n\t"
+            "madc.lo.cc.u32 %4, %13, %16, %4;\n\t"
+            "madc.hi.cc.u32 %5, %13, %16, %5;\n\t"
+            "madc.lo.cc.u32 %6, %13, %17, %6;\n\t"
+            "madc.hi.cc.u32 %7, %13, %17, %7;\n\t"
+            "madc.lo.cc.u32 %8, %13, %18, %8;\n\t"
+            "madc.hi.cc.u32 %9, %13, %18, %9;\n\t"
+            "madc.lo.cc.u32 %10, %13, %19, %10;\n\t"
+            "madc.hi.cc.u32 %11, %13, %19, %11;\n\t"
+            "addc.u32       %12, %12, 0;"
+            : "+r"(e[0]), "+r"(e[1]), "+r"(e[2]), "+r"(e[3]), "+r"(e[4]), "+r"(e[5]),
+              "+r"(e[6]), "+r"(e[7]), "+r"(e[8]), "+r"(e[9]), "+r"(e[10]), "+r"(e[11]),
+              "+r"(e[12])
+            : "r"(m), "n"(CATMSM_P0), "n"(CATMSM_P2), "n"(CATMSM_P4), "n"(CATMSM_P6),
+              "n"(CATMSM_P8), "n"(CATMSM_P10));
+        asm("mad.lo.cc.u32  %0, %13, %14, %0;\n\t"
+            "madc.hi.cc.u32 %1, %13, %14, %1;\n\t"
+            "madc.lo.cc.u32 %2, %13, %15, %2;\n\t"
+            "madc.hi.cc.u32 %3, %13, %15, %3;\n\t"
+            "madc.lo.cc.u32 %4, %13, %16, %4;\n\t"
+            "madc.hi.cc.u32 %5, %13, %16, %5;\n\t"
+            "madc.lo.cc.u32 %6, %13, %17, %6;\n\t"
+            "madc.hi.cc.u32 %7, %13, %17, %7;\n\t"
+            "madc.lo.cc.u32 %8, %13, %18, %8;\n\t"
+            "madc.hi.cc.u32 %9, %13, %18, %9;\n\t"
+            "madc.lo.cc.u32 %10, %13, %19, %10;\n\t"
+            "madc.hi.cc.u32 %11, %13, %19, %11;\n\t"
+            "addc.u32       %12, 0, 0;"
+            : "+r"(o[0]), "+r"(o[1]), "+r"(o[2]), "+r"(o[3]), "+r"(o[4]), "+r"(o[5]),
+              "+r"(o[6]), "+r"(o[7]), "+r"(o[8]), "+r"(o[9]), "+r"(o[10]), "+r"(o[11]),
+              "=r"(o[12])
+            : "r"(m), "n"(CATMSM_P1), "n"(CATMSM_P3), "n"(CATMSM_P5), "n"(CATMSM_P7),
+              "n"(CATMSM_P9), "n"(CATMSM_P11));
+        asm("add.cc.u32  %0, %0, %12;\n\t"
+            "addc.cc.u32 %1, %1, %13;\n\t"
+            "addc.cc.u32 %2, %2, %14;\n\t"
+            "addc.cc.u32 %3, %3, %15;\n\t"
+            "addc.cc.u32 %4, %4, %16;\n\t"
+            "addc.cc.u32 %5, %5, %17;\n\t"
+            "addc.cc.u32 %6, %6, %18;\n\t"
+            "addc.cc.u32 %7, %7, %19;\n\t"
+            "addc.cc.u32 %8, %8, %20;\n\t"
+            "addc.cc.u32 %9, %9, %21;\n\t"
+            "addc.cc.u32 %10, %10, %22;\n\t"
+            "addc.u32    %11, %11, %23;"
+            : "+r"(o[0]), "+r"(o[1]), "+r"(o[2]), "+r"(o[3]), "+r"(o[4]), "+r"(o[5]),
+              "+r"(o[6]), "+r"(o[7]), "+r"(o[8]), "+r"(o[9]), "+r"(o[10]), "+r"(o[11])
+            : "r"(e[1]), "r"(e[2]), "r"(e[3]), "r"(e[4]), "r"(e[5]), "r"(e[6]),
+              "r"(e[7]), "r"(e[8]), "r"(e[9]), "r"(e[10]), "r"(e[11]), "r"(e[12]));
+#pragma unroll
+        for (int k = 0; k < 12; k++) t[k] = o[k];
+    }
+    {   // step 3
+        const uint32_t bi = a.v[3];
+#pragma unroll
+        for (int k = 0; k < 12; k++) e[k] = t[k];
+        asm("mad.lo.cc.u32  %0, %9, %13, %0;\n\t"
+            "madc.hi.cc.u32 %1, %9, %13, %1;\n\t"
+            "madc.lo.cc.u32 %2, %10, %13, %2;\n\t"
+            "madc.hi.cc.u32 %3, %10, %13, %3;\n\t"
+            "madc.lo.cc.u32 %4, %11, %13, %4;\n\t"
+            "madc.hi.cc.u32 %5, %11, %13, %5;\n\t"
+            "madc.lo.cc.u32 %6, %12, %13, %6;\n\t"
+            "madc.hi.cc.u32 %7, %12, %13, %7;\n\t"
+            "addc.u32       %8, 0, 0;"
+            : "+r"(e[4]), "+r"(e[5]), "+r"(e[6]), "+r"(e[7]), "+r"(e[8]), "+r"(e[9]), "+r"(e[10]), "+r"(e[11]), "=r"(e[12])
+            : "r"((a.v[4] << 1)), "r"(d[6]), "r"(d[8]), "r"(d[10]), "r"(bi));
+#pragma unroll
+        for (int k = 0; k < 13; k++) o[k] = 0;
+        o[2] = a.v[3] * bi;
+        o[3] = __umulhi(a.v[3], bi);
+        o[4] = d[5] * bi;
+        o[5] = __umulhi(d[5], bi);
+        o[6] = d[7] * bi;
+        o[7] = __umulhi(d[7], bi);
+        o[8] = d[9] * bi;
+        o[9] = __umulhi(d[9], bi);
+        o[10] = d[11] * bi;
+        o[11] = __umulhi(d[11], bi);
+        const uint32_t m = e[0] * CATMSM_N0;
+        asm("mad.lo.cc.u32  %0, %13, %14, %0;\n\t"
+            "madc.hi.cc.u32 %1, %13, %14, %1;\n\t"
+            "madc.lo.cc.u32 %2, %13, %15, %2;\n\t"
+            "madc.hi.cc.u32 %3, %13, %15, %3;\n\t"
+            "madc.lo.cc.u32 %4, %13, %16, %4;\n\t"
+            "madc.hi.cc.u32 %5, %13, %16, %5;\n\t"
+            "madc.lo.cc.u32 %6, %13, %17, %6;\n\t"
+            "madc.hi.cc.u32 %7, %13, %17, %7;\n\t"
+            "madc.lo.cc.u32 %8, %13, %18, %8;\n\t"
+            "madc.hi.cc.u32 %9, %13, %18, %9;\n\t"
+            "madc.lo.cc.u32 %10, %13, %19, %10;\n\t"
+            "madc.hi.cc.u32 %11, %13, %19, %11;\n\t"
+            "addc.u32       %12, %12, 0;"
+            : "+r"(e[0]), "+r"(e[1]), "+r"(e[2]), "+r"(e[3]), "+r"(e[4]), "+r"(e[5]),
+              "+r"(e[6]), "+r"(e[7]), "+r"(e[8]), "+r"(e[9]), "+r"(e[10]), "+r"(e[11]),
+              "+r"(e[12])
+            : "r"(m), "n"(CATMSM_P0), "n"(CATMSM_P2), "n"(CATMSM_P4), "n"(CATMSM_P6),
+              "n"(CATMSM_P8), "n"(CATMSM_P10));
+        asm("mad.lo.cc.u32  %0, %13, %14, %0;\n\t"
+            "madc.hi.cc.u32 %1, %13, %14, %1;\n\t"
+            "madc.lo.cc.u32 %2, %13, %15, %2;\n\t"
+            "madc.hi.cc.u32 %3, %13, %15, %3;\n\t"
+            "madc.lo.cc.u32 %4, %13, %16, %4;\n\t"
+            "madc.hi.cc.u32 %5, %13, %16, %5;\n\t"
+            "madc.lo.cc.u32 %6, %13, %17, %6;\n\t"
+            "madc.hi.cc.u32 %7, %13, %17, %7;\n\t"
+            "madc.lo.cc.u32 %8, %13, %18, %8;\n\t"
+            "madc.hi.cc.u32 %9, %13, %18, %9;\n\t"
+            "madc.lo.cc.u32 %10, %13, %19, %10;\n\t"
+            "madc.hi.cc.u32 %11, %13, %19, %11;\n\t"
+            "addc.u32       %12, 0, 0;"
+            : "+r"(o[0]), "+r"(o[1]), "+r"(o[2]), "+r"(o[3]), "+r"(o[4]), "+r"(o[5]),
+              "+r"(o[6]), "+r"(o[7]), "+r"(o[8]), "+r"(o[9]), "+r"(o[10]), "+r"(o[11]),
+              "=r"(o[12])
+            : "r"(m), "n"(CATMSM_P1), "n"(CATMSM_P3), "n"(CATMSM_P5), "n"(CATMSM_P7),
+              "n"(CATMSM_P9), "n"(CATMSM_P11));
+        asm("add.cc.u32  %0, %0, %12;\n\t"
+            "addc.cc.u32 %1, %1, %13;\n\t"
+            "addc.cc.u32 %2, %2, %14;\n\t"
+            "addc.cc.u32 %3, %3, %15;\n\t"
+            "addc.cc.u32 %4, %4, %16;\n\t"
+            "addc.cc.u32 %5, %5, %17;\n\t"
+            "addc.cc.u32 %6, %6, %18;\n\t"
+            "addc.cc.u32 %7, %7, %19;\n\t"
+            "addc.cc.u32 %8, %8, %20;\n\t"
+            "addc.cc.u32 %9, %9, %21;\n\t"
+            "addc.cc.u32 %10, %10, %22;\n\t"
+            "addc.u32    %11, %11, %23;"
+            : "+r"(o[0]), "+r"(o[1]), "+r"(o[2]), "+r"(o[3]), "+r"(o[4]), "+r"(o[5]),
+              "+r"(o[6]), "+r"(o[7]), "+r"(o[8]), "+r"(o[9]), "+r"(o[10]), "+r"(o[11])
+            : "r"(e[1]), "r"(e[2]), "r"(e[3]), "r"(e[4]), "r"(e[5]), "r"(e[6]),
+              "r"(e[7]), "r"(e[8]), "r"(e[9]), "r"(e[10]), "r"(e[11]), "r"(e[12]));
+#pragma unroll
+        for (int k = 0; k < 12; k++) t[k] = o[k];
+    }
+    {   // step 4
+        const uint32_t bi = a.v[4];
+#pragma unroll
+        for (int k = 0; k < 12; k++) e[k] = t[k];
+        asm("mad.lo.cc.u32  %0, %9, %13, %0;\n\t"
+            "madc.hi.cc.u32 %1, %9, %13, %1;\n\t"
+            "madc.lo.cc.u32 %2, %10, %13, %2;\n\t"
+            "madc.hi.cc.u32 %3, %10, %13, %3;\n\t"
+            "madc.lo.cc.u32 %4, %11, %13, %4;\n\t"
+            "madc.hi.cc.u32 %5, %11, %13, %5;\n\t"
+            "madc.lo.cc.u32 %6, %12, %13, %6;\n\t"
+            "madc.hi.cc.u32 %7, %12, %13, %7;\n\t"
+            "addc.u32       %8, 0, 0;"
+            : "+r"(e[4]), "+r"(e[5]), "+r"(e[6]), "+r"(e[7]), "+r"(e[8]), "+r"(e[9]), "+r"(e[10]), "+r"(e[11]), "=r"(e[12])
+            : "r"(a.v[4]), "r"(d[6]), "r"(d[8]), "r"(d[10]), "r"(bi));
+#pragma unroll
+        for (int k = 0; k < 13; k++) o[k] = 0;
+        o[4] = (a.v[5] << 1) * bi;
+        o[5] = __umulhi((a.v[5] << 1), bi);
+        o[6] = d[7] * bi;
+        o[7] = __umulhi(d[7], bi);
+        o[8] = d[9] * bi;
+        o[9] = __umulhi(d[9], bi);
+        o[10] = d[11] * bi;
+        o[11] = __umulhi(d[11], bi);
+        const uint32_t m = e[0] * CATMSM_N0;
+        asm("mad.lo.cc.u32  %0, %13, %14, %0;\n\t"
+            "madc.hi.cc.u32 %1, %13, %14, %1;\n\t"
+            "madc.lo.cc.u32 %2, %13, %15, %2;\n\t"
+            "madc.hi.cc.u32 %3, %13, %15, %3;\n\t"
+            "madc.lo.cc.u32 %4, %13, %16, %4;\n\t"
+            "madc.hi.cc.u32 %5, %13, %16, %5;\n\t"
+            "madc.lo.cc.u32 %6, %13, %17, %6;\n\t"
+            "madc.hi.cc.u32 %7, %13, %17, %7;\n\t"
+            "madc.lo.cc.u32 %8, %13, %18, %8;\n\t"
+            "madc.hi.cc.u32 %9, %13, %18, %9;\n\t"
+            "madc.lo.cc.u32 %10, %13, %19, %10;\n\t"
+            "madc.hi.cc.u32 %11, %13, %19, %11;\n\t"
+            "addc.u32       %12, %12, 0;"
+            : "+r"(e[0]), "+r"(e[1]), "+r"(e[2]), "+r"(e[3]), "+r"(e[4]), "+r"(e[5]),
+              "+r"(e[6]), "+r"(e[7]), "+r"(e[8]), "+r"(e[9]), "+r"(e[10]), "+r"(e[11]),
+              "+r"(e[12])
+            : "r"(m), "n"(CATMSM_P0), "n"(CATMSM_P2), "n"(CATMSM_P4), "n"(CATMSM_P6),
+              "n"(CATMSM_P8), "n"(CATMSM_P10));
+        asm("mad.lo.cc.u32  %0, %13, %14, %0;\n\t"
+            "madc.hi.cc.u32 %1, %13, %14, %1;\n\t"
+            "madc.lo.cc.u32 %2, %13, %15, %2;\n\t"
+            "madc.hi.cc.u32 %3, %13, %15, %3;\n\t"
+            "madc.lo.cc.u32 %4, %13, %16, %4;\n\t"
+            "madc.hi.cc.u32 %5, %13, %16, %5;\n\t"
+            "madc.lo.cc.u32 %6, %13, %17, %6;\n\t"
+            "madc.hi.cc.u32 %7, %13, %17, %7;\n\t"
+            "madc.lo.cc.u32 %8, %13, %18, %8;\n\t"
+            "madc.hi.cc.u32 %9, %13, %18, %9;\n\t"
+            "madc.lo.cc.u32 %10, %13, %19, %10;\n\t"
+            "madc.hi.cc.u32 %11, %13, %19, %11;\n\t"
+            "addc.u32       %12, 0, 0;"
+            : "+r"(o[0]), "+r"(o[1]), "+r"(o[2]), "+r"(o[3]), "+r"(o[4]), "+r"(o[5]),
+              "+r"(o[6]), "+r"(o[7]), "+r"(o[8]), "+r"(o[9]), "+r"(o[10]), "+r"(o[11]),
+              "=r"(o[12])
+            : "r"(m), "n"(CATMSM_P1), "n"(CATMSM_P3), "n"(CATMSM_P5), "n"(CATMSM_P7),
+              "n"(CATMSM_P9), "n"(CATMSM_P11));
+        asm("add.cc.u32  %0, %0, %12;\n\t"
+            "addc.cc.u32 %1, %1, %13;\n\t"
+            "addc.cc.u32 %2, %2, %14;\n\t"
+            "addc.cc.u32 %3, %3, %15;\n\t"
+            "addc.cc.u32 %4, %4, %16;\n\t"
+            "addc.cc.u32 %5, %5, %17;\n\t"
+            "addc.cc.u32 %6, %6, %18;\n\t"
+            "addc.cc.u32 %7, %7, %19;\n\t"
+            "addc.cc.u32 %8, %8, %20;\n\t"
+            "addc.cc.u32 %9, %9, %21;\n\t"
+            "addc.cc.u32 %10, %10, %22;\n\t"
+            "addc.u32    %11, %11, %23;"
+            : "+r"(o[0]), "+r"(o[1]), "+r"(o[2]), "+r"(o[3]), "+r"(o[4]), "+r"(o[5]),
+              "+r"(o[6]), "+r"(o[7]), "+r"(o[8]), "+r"(o[9]), "+r"(o[10]), "+r"(o[11])
+            : "r"(e[1]), "r"(e[2]), "r"(e[3]), "r"(e[4]), "r"(e[5]), "r"(e[6]),
+              "r"(e[7]), "r"(e[8]), "r"(e[9]), "r"(e[10]), "r"(e[11]), "r"(e[12]));
+#pragma unroll
+        for (int k = 0; k < 12; k++) t[k] = o[k];
+    }
+    {   // step 5
+        const uint32_t bi = a.v[5];
+#pragma unroll
+        for (int k = 0; k < 12; k++) e[k] = t[k];
+        asm("mad.lo.cc.u32  %0, %7, %10, %0;\n\t"
+            "madc.hi.cc.u32 %1, %7, %10, %1;\n\t"
+            "madc.lo.cc.u32 %2, %8, %10, %2;\n\t"
+            "madc.hi.cc.u32 %3, %8, %10, %3;\n\t"
+            "madc.lo.cc.u32 %4, %9, %10, %4;\n\t"
+            "madc.hi.cc.u32 %5, %9, %10, %5;\n\t"
+            "addc.u32       %6, 0, 0;"
+            : "+r"(e[6]), "+r"(e[7]), "+r"(e[8]), "+r"(e[9]), "+r"(e[10]), "+r"(e[11]), "=r"(e[12])
+            : "r"((a.v[6] << 1)), "r"(d[8]), "r"(d[10]), "r"(bi));
+#pragma unroll
+        for (int k = 0; k < 13; k++) o[k] = 0;
+        o[4] = a.v[5] * bi;
+        o[5] = __umulhi(a.v[5], bi);
+        o[6] = d[7] * bi;
+        o[7] = __umulhi(d[7], bi);
+        o[8] = d[9] * bi;
+        o[9] = __umulhi(d[9], bi);
+        o[10] = d[11] * bi;
+        o[11] = __umulhi(d[11], bi);
+        const uint32_t m = e[0] * CATMSM_N0;
+        asm("mad.lo.cc.u32  %0, %13, %14, %0;\n\t"
+            "madc.hi.cc.u32 %1, %13, %14, %1;\n\t"
+            "madc.lo.cc.u32 %2, %13, %15, %2;\n\t"
+            "madc.hi.cc.u32 %3, %13, %15, %3;\n\t"
+            "madc.lo.cc.u32 %4, %13, %16, %4;\n\t"
+            "madc.hi.cc.u32 %5, %13, %16, %5;\n\t"
+            "madc.lo.cc.u32 %6, %13, %17, %6;\n\t"
+            "madc.hi.cc.u32 %7, %13, %17, %7;\n\t"
+            "madc.lo.cc.u32 %8, %13, %18, %8;\n\t"
+            "madc.hi.cc.u32 %9, %13, %18, %9;\n\t"
+            "madc.lo.cc.u32 %10, %13, %19, %10;\n\t"
+            "madc.hi.cc.u32 %11, %13, %19, %11;\n\t"
+            "addc.u32       %12, %12, 0;"
+            : "+r"(e[0]), "+r"(e[1]), "+r"(e[2]), "+r"(e[3]), "+r"(e[4]), "+r"(e[5]),
+              "+r"(e[6]), "+r"(e[7]), "+r"(e[8]), "+r"(e[9]), "+r"(e[10]), "+r"(e[11]),
+              "+r"(e[12])
+            : "r"(m), "n"(CATMSM_P0), "n"(CATMSM_P2), "n"(CATMSM_P4), "n"(CATMSM_P6),
+              "n"(CATMSM_P8), "n"(CATMSM_P10));
+        asm("mad.lo.cc.u32  %0, %13, %14, %0;\n\t"
+            "madc.hi.cc.u32 %1, %13, %14, %1;\n\t"
+            "madc.lo.cc.u32 %2, %13, %15, %2;\n\t"
+            "madc.hi.cc.u32 %3, %13, %15, %3;\n\t"
+            "madc.lo.cc.u32 %4, %13, %16, %4;\n\t"
+            "madc.hi.cc.u32 %5, %13, %16, %5;\n\t"
+            "madc.lo.cc.u32 %6, %13, %17, %6;\n\t"
+            "madc.hi.cc.u32 %7, %13, %17, %7;\n\t"
+            "madc.lo.cc.u32 %8, %13, %18, %8;\n\t"
+            "madc.hi.cc.u32 %9, %13, %18, %9;\n\t"
+            "madc.lo.cc.u32 %10, %13, %19, %10;\n\t"
+            "madc.hi.cc.u32 %11, %13, %19, %11;\n\t"
+            "addc.u32       %12, 0, 0;"
+            : "+r"(o[0]), "+r"(o[1]), "+r"(o[2]), "+r"(o[3]), "+r"(o[4]), "+r"(o[5]),
+              "+r"(o[6]), "+r"(o[7]), "+r"(o[8]), "+r"(o[9]), "+r"(o[10]), "+r"(o[11]),
+              "=r"(o[12])
+            : "r"(m), "n"(CATMSM_P1), "n"(CATMSM_P3), "n"(CATMSM_P5), "n"(CATMSM_P7),
+              "n"(CATMSM_P9), "n"(CATMSM_P11));
+        asm("add.cc.u32  %0, %0, %12;\n\t"
+            "addc.cc.u32 %1, %1, %13;\n\t"
+            "addc.cc.u32 %2, %2, %14;\n\t"
+            "addc.cc.u32 %3, %3, %15;\n\t"
+            "addc.cc.u32 %4, %4, %16;\n\t"
+            "addc.cc.u32 %5, %5, %17;\n\t"
+            "addc.cc.u32 %6, %6, %18;\n\t"
+            "addc.cc.u32 %7, %7, %19;\n\t"
+            "addc.cc.u32 %8, %8, %20;\n\t"
+            "addc.cc.u32 %9, %9, %21;\n\t"
+            "addc.cc.u32 %10, %10, %22;\n\t"
+            "addc.u32    %11, %11, %23;"
+            : "+r"(o[0]), "+r"(o[1]), "+r"(o[2]), "+r"(o[3]), "+r"(o[4]), "+r"(o[5]),
+              "+r"(o[6]), "+r"(o[7]), "+r"(o[8]), "+r"(o[9]), "+r"(o[10]), "+r"(o[11])
+            : "r"(e[1]), "r"(e[2]), "r"(e[3]), "r"(e[4]), "r"(e[5]), "r"(e[6]),
+              "r"(e[7]), "r"(e[8]), "r"(e[9]), "r"(e[10]), "r"(e[11]), "r"(e[12]));
+#pragma unroll
+        for (int k = 0; k < 12; k++) t[k] = o[k];
+    }
+    {   // step 6
+        const uint32_t bi = a.v[6];
+#pragma unroll
+        for (int k = 0; k < 12; k++) e[k] = t[k];
+        asm("mad.lo.cc.u32  %0, %7, %10, %0;\n\t"
+            "madc.hi.cc.u32 %1, %7, %10, %1;\n\t"
+            "madc.lo.cc.u32 %2, %8, %10, %2;\n\t"
+            "madc.hi.cc.u32 %3, %8, %10, %3;\n\t"
+            "madc.lo.cc.u32 %4, %9, %10, %4;\n\t"
+            "madc.hi.cc.u32 %5, %9, %10, %5;\n\t"
+            "addc.u32       %6, 0, 0;"
+            : "+r"(e[6]), "+r"(e[7]), "+r"(e[8]), "+r"(e[9]), "+r"(e[10]), "+r"(e[11]), "=r"(e[12])
+            : "r"(a.v[6]), "r"(d[8]), "r"(d[10]), "r"(bi));
+#pragma unroll
+        for (int k = 0; k < 13; k++) o[k] = 0;
+        o[6] = (a.v[7] << 1) * bi;
+        o[7] = __umulhi((a.v[7] << 1), bi);
+        o[8] = d[9] * bi;
+        o[9] = __umulhi(d[9], bi);
+        o[10] = d[11] * bi;
+        o[11] = __umulhi(d[11], bi);
+        const uint32_t m = e[0] * CATMSM_N0;
+        asm("mad.lo.cc.u32  %0, %13, %14, %0;\n\t"
+            "madc.hi.cc.u32 %1, %13, %14, %1;\n\t"
+            "madc.lo.cc.u32 %2, %13, %15, %2;\n\t"
+            "madc.hi.cc.u32 %3, %13, %15, %3;\n\t"
+            "madc.lo.cc.u32 %4, %13, %16, %4;\n\t"
+            "madc.hi.cc.u32 %5, %13, %16, %5;\n\t"
+            "madc.lo.cc.u32 %6, %13, %17, %6;\n\t"
+            "madc.hi.cc.u32 %7, %13, %17, %7;\n\t"
+            "madc.lo.cc.u32 %8, %13, %18, %8;\n\t"
+            "madc.hi.cc.u32 %9, %13, %18, %9;\n\t"
+            "madc.lo.cc.u32 %10, %13, %19, %10;\n\t"
+            "madc.hi.cc.u32 %11, %13, %19, %11;\n\t"
+            "addc.u32       %12, %12, 0;"
+            : "+r"(e[0]), "+r"(e[1]), "+r"(e[2]), "+r"(e[3]), "+r"(e[4]), "+r"(e[5]),
+              "+r"(e[6]), "+r"(e[7]), "+r"(e[8]), "+r"(e[9]), "+r"(e[10]), "+r"(e[11]),
+              "+r"(e[12])
+            : "r"(m), "n"(CATMSM_P0), "n"(CATMSM_P2), "n"(CATMSM_P4), "n"(CATMSM_P6),
+              "n"(CATMSM_P8), "n"(CATMSM_P10));
+        asm("mad.lo.cc.u32  %0, %13, %14, %0;\n\t"
+            "madc.hi.cc.u32 %1, %13, %14, %1;\n\t"
+            "madc.lo.cc.u32 %2, %13, %15, %2;\n\t"
+            "madc.hi.cc.u32 %3, %13, %15, %3;\n\t"
+            "madc.lo.cc.u32 %4, %13, %16, %4;\n\t"
+            "madc.hi.cc.u32 %5, %13, %16, %5;\n\t"
+            "madc.lo.cc.u32 %6, %13, %17, %6;\n\t"
+            "madc.hi.cc.u32 %7, %13, %17, %7;\n\t"
+            "madc.lo.cc.u32 %8, %13, %18, %8;\n\t"
+            "madc.hi.cc.u32 %9, %13, %18, %9;\n\t"
+            "madc.lo.cc.u32 %10, %13, %19, %10;\n\t"
+            "madc.hi.cc.u32 %11, %13, %19, %11;\n\t"
+            "addc.u32       %12, 0, 0;"
+            : "+r"(o[0]), "+r"(o[1]), "+r"(o[2]), "+r"(o[3]), "+r"(o[4]), "+r"(o[5]),
+              "+r"(o[6]), "+r"(o[7]), "+r"(o[8]), "+r"(o[9]), "+r"(o[10]), "+r"(o[11]),
+              "=r"(o[12])
+            : "r"(m), "n"(CATMSM_P1), "n"(CATMSM_P3), "n"(CATMSM_P5), "n"(CATMSM_P7),
+              "n"(CATMSM_P9), "n"(CATMSM_P11));
+        asm("add.cc.u32  %0, %0, %12;\n\t"
+            "addc.cc.u32 %1, %1, %13;\n\t"
+            "addc.cc.u32 %2, %2, %14;\n\t"
+            "addc.cc.u32 %3, %3, %15;\n\t"
+            "addc.cc.u32 %4, %4, %16;\n\t"
+            "addc.cc.u32 %5, %5, %17;\n\t"
+            "addc.cc.u32 %6, %6, %18;\n\t"
+            "addc.cc.u32 %7, %7, %19;\n\t"
+            "addc.cc.u32 %8, %8, %20;\n\t"
+            "addc.cc.u32 %9, %9, %21;\n\t"
+            "addc.cc.u32 %10, %10, %22;\n\t"
+            "addc.u32    %11, %11, %23;"
+            : "+r"(o[0]), "+r"(o[1]), "+r"(o[2]), "+r"(o[3]), "+r"(o[4]), "+r"(o[5]),
+              "+r"(o[6]), "+r"(o[7]), "+r"(o[8]), "+r"(o[9]), "+r"(o[10]), "+r"(o[11])
+            : "r"(e[1]), "r"(e[2]), "r"(e[3]), "r"(e[4]), "r"(e[5]), "r"(e[6]),
+              "r"(e[7]), "r"(e[8]), "r"(e[9]), "r"(e[10]), "r"(e[11]), "r"(e[12]));
+#pragma unroll
+        for (int k = 0; k < 12; k++) t[k] = o[k];
+    }
+    {   // step 7
+        const uint32_t bi = a.v[7];
+#pragma unroll
+        for (int k = 0; k < 12; k++) e[k] = t[k];
+        asm("mad.lo.cc.u32  %0, %5, %7, %0;\n\t"
+            "madc.hi.cc.u32 %1, %5, %7, %1;\n\t"
+            "madc.lo.cc.u32 %2, %6, %7, %2;\n\t"
+            "madc.hi.cc.u32 %3, %6, %7, %3;\n\t"
+            "addc.u32       %4, 0, 0;"
+            : "+r"(e[8]), "+r"(e[9]), "+r"(e[10]), "+r"(e[11]), "=r"(e[12])
+            : "r"((a.v[8] << 1)), "r"(d[10]), "r"(bi));
+#pragma unroll
+        for (int k = 0; k < 13; k++) o[k] = 0;
+        o[6] = a.v[7] * bi;
+        o[7] = __umulhi(a.v[7], bi);
+        o[8] = d[9] * bi;
+        o[9] = __umulhi(d[9], bi);
+        o[10] = d[11] * bi;
+        o[11] = __umulhi(d[11], bi);
+        const uint32_t m = e[0] * CATMSM_N0;
+        asm("mad.lo.cc.u32  %0, %13, %14, %0;\n\t"
+            "madc.hi.cc.u32 %1, %13, %14, %1;\n\t"
+            "madc.lo.cc.u32 %2, %13, %15, %2;\n\t"
+            "madc.hi.cc.u32 %3, %13, %15, %3;\n\t"
+            "madc.lo.cc.u32 %4, %13, %16, %4;\n\t"
+            "madc.hi.cc.u32 %5, %13, %16, %5;\n\t"
+            "madc.lo.cc.u32 %6, %13, %17, %6;\n\t"
+            "madc.hi.cc.u32 %7, %13, %17, %7;\n\t"
+            "madc.lo.cc.u32 %8, %13, %18, %8;\n\t"
+            "madc.hi.cc.u32 %9, %13, %18, %9;\n\t"
+            "madc.lo.cc.u32 %10, %13, %19, %10;\n\t"
+            "madc.hi.cc.u32 %11, %13, %19, %11;\n\t"
+            "addc.u32       %12, %12, 0;"
+            : "+r"(e[0]), "+r"(e[1]), "+r"(e[2]), "+r"(e[3]), "+r"(e[4]), "+r"(e[5]),
+              "+r"(e[6]), "+r"(e[7]), "+r"(e[8]), "+r"(e[9]), "+r"(e[10]), "+r"(e[11]),
+              "+r"(e[12])
+            : "r"(m), "n"(CATMSM_P0), "n"(CATMSM_P2), "n"(CATMSM_P4), "n"(CATMSM_P6),
+              "n"(CATMSM_P8), "n"(CATMSM_P10));
+        asm("mad.lo.cc.u32  %0, %13, %14, %0;\n\t"
+            "madc.hi.cc.u32 %1, %13, %14, %1;\n\t"
+            "madc.lo.cc.u32 %2, %13, %15, %2;\n\t"
+            "madc.hi.cc.u32 %3, %13, %15, %3;\n\t"
+            "madc.lo.cc.u32 %4, %13, %16, %4;\n\t"
+            "madc.hi.cc.u32 %5, %13, %16, %5;\n\t"
+            "madc.lo.cc.u32 %6, %13, %17, %6;\n\t"
+            "madc.hi.cc.u32 %7, %13, %17, %7;\n\t"
+            "madc.lo.cc.u32 %8, %13, %18, %8;\n\t"
+            "madc.hi.cc.u32 %9, %13, %18, %9;\n\t"
+            "madc.lo.cc.u32 %10, %13, %19, %10;\n\t"
+            "madc.hi.cc.u32 %11, %13, %19, %11;\n\t"
+            "addc.u32       %12, 0, 0;"
+            : "+r"(o[0]), "+r"(o[1]), "+r"(o[2]), "+r"(o[3]), "+r"(o[4]), "+r"(o[5]),
+              "+r"(o[6]), "+r"(o[7]), "+r"(o[8]), "+r"(o[9]), "+r"(o[10]), "+r"(o[11]),
+              "=r"(o[12])
+            : "r"(m), "n"(CATMSM_P1), "n"(CATMSM_P3), "n"(CATMSM_P5), "n"(CATMSM_P7),
+              "n"(CATMSM_P9), "n"(CATMSM_P11));
+        asm("add.cc.u32  %0, %0, %12;\n\t"
+            "addc.cc.u32 %1, %1, %13;\n\t"
+            "addc.cc.u32 %2, %2, %14;\n\t"
+            "addc.cc.u32 %3, %3, %15;\n\t"
+            "addc.cc.u32 %4, %4, %16;\n\t"
+            "addc.cc.u32 %5, %5, %17;\n\t"
+            "addc.cc.u32 %6, %6, %18;\n\t"
+            "addc.cc.u32 %7, %7, %19;\n\t"
+            "addc.cc.u32 %8, %8, %20;\n\t"
+            "addc.cc.u32 %9, %9, %21;\n\t"
+            "addc.cc.u32 %10, %10, %22;\n\t"
+            "addc.u32    %11, %11, %23;"
+            : "+r"(o[0]), "+r"(o[1]), "+r"(o[2]), "+r"(o[3]), "+r"(o[4]), "+r"(o[5]),
+              "+r"(o[6]), "+r"(o[7]), "+r"(o[8]), "+r"(o[9]), "+r"(o[10]), "+r"(o[11])
+            : "r"(e[1]), "r"(e[2]), "r"(e[3]), "r"(e[4]), "r"(e[5]), "r"(e[6]),
+              "r"(e[7]), "r"(e[8]), "r"(e[9]), "r"(e[10]), "r"(e[11]), "r"(e[12]));
+#pragma unroll
+        for (int k = 0; k < 12; k++) t[k] = o[k];
+    }
+    {   // step 8
+        const uint32_t bi = a.v[8];
+#pragma unroll
+        for (int k = 0; k < 12; k++) e[k] = t[k];
+        asm("mad.lo.cc.u32  %0, %5, %7, %0;\n\t"
+            "madc.hi.cc.u32 %1, %5, %7, %1;\n\t"
+            "madc.lo.cc.u32 %2, %6, %7, %2;\n\t"
+            "madc.hi.cc.u32 %3, %6, %7, %3;\n\t"
+            "addc.u32       %4, 0, 0;"
+            : "+r"(e[8]), "+r"(e[9]), "+r"(e[10]), "+r"(e[11]), "=r"(e[12])
+            : "r"(a.v[8]), "r"(d[10]), "r"(bi));
+#pragma unroll
+        for (int k = 0; k < 13; k++) o[k] = 0;
+        o[8] = (a.v[9] << 1) * bi;
+        o[9] = __umulhi((a.v[9] << 1), bi);
+        o[10] = d[11] * bi;
+        o[11] = __umulhi(d[11], bi);
+        const uint32_t m = e[0] * CATMSM_N0;
+        asm("mad.lo.cc.u32  %0, %13, %14, %0;\n\t"
+            "madc.hi.cc.u32 %1, %13, %14, %1;\n\t"
+            "madc.lo.cc.u32 %2, %13, %15, %2;\n\t"
+            "madc.hi.cc.u32 %3, %13, %15, %3;\n\t"
+            "madc.lo.cc.u32 %4, %13, %16, %4;\n\t"
+            "madc.hi.cc.u32 %5, %13, %16, %5;\n\t"
+            "madc.lo.cc.u32 %6, %13, %17, %6;\n\t"
+            "madc.hi.cc.u32 %7, %13, %17, %7;\n\t"
+            "madc.lo.cc.u32 %8, %13, %18, %8;\n\t"
+            "madc.hi.cc.u32 %9, %13, %18, %9;\n\t"
+            "madc.lo.cc.u32 %10, %13, %19, %10;\n\t"
+            "madc.hi.cc.u32 %11, %13, %19, %11;\n\t"
+            "addc.u32       %12, %12, 0;"
+            : "+r"(e[0]), "+r"(e[1]), "+r"(e[2]), "+r"(e[3]), "+r"(e[4]), "+r"(e[5]),
+              "+r"(e[6]), "+r"(e[7]), "+r"(e[8]), "+r"(e[9]), "+r"(e[10]), "+r"(e[11]),
+              "+r"(e[12])
+            : "r"(m), "n"(CATMSM_P0), "n"(CATMSM_P2), "n"(CATMSM_P4), "n"(CATMSM_P6),
+              "n"(CATMSM_P8), "n"(CATMSM_P10));
+        asm("mad.lo.cc.u32  %0, %13, %14, %0;\n\t"
+            "madc.hi.cc.u32 %1, %13, %14, %1;\n\t"
+            "madc.lo.cc.u32 %2, %13, %15, %2;\n\t"
+            "madc.hi.cc.u32 %3, %13, %15, %3;\n\t"
+            "madc.lo.cc.u32 %4, %13, %16, %4;\n\t"
+            "madc.hi.cc.u32 %5, %13, %16, %5;\n\t"
+            "madc.lo.cc.u32 %6, %13, %17, %6;\n\t"
+            "madc.hi.cc.u32 %7, %13, %17, %7;\n\t"
+            "madc.lo.cc.u32 %8, %13, %18, %8;\n\t"
+            "madc.hi.cc.u32 %9, %13, %18, %9;\n\t"
+            "madc.lo.cc.u32 %10, %13, %19, %10;\n\t"
+            "madc.hi.cc.u32 %11, %13, %19, %11;\n\t"
+            "addc.u32       %12, 0, 0;"
+            : "+r"(o[0]), "+r"(o[1]), "+r"(o[2]), "+r"(o[3]), "+r"(o[4]), "+r"(o[5]),
+              "+r"(o[6]), "+r"(o[7]), "+r"(o[8]), "+r"(o[9]), "+r"(o[10]), "+r"(o[11]),
+              "=r"(o[12])
+            : "r"(m), "n"(CATMSM_P1), "n"(CATMSM_P3), "n"(CATMSM_P5), "n"(CATMSM_P7),
+              "n"(CATMSM_P9), "n"(CATMSM_P11));
+        asm("add.cc.u32  %0, %0, %12;\n\t"
+            "addc.cc.u32 %1, %1, %13;\n\t"
+            "addc.cc.u32 %2, %2, %14;\n\t"
+            "addc.cc.u32 %3, %3, %15;\n\t"
+            "addc.cc.u32 %4, %4, %16;\n\t"
+            "addc.cc.u32 %5, %5, %17;\n\t"
+            "addc.cc.u32 %6, %6, %18;\n\t"
+            "addc.cc.u32 %7, %7, %19;\n\t"
+            "addc.cc.u32 %8, %8, %20;\n\t"
+            "addc.cc.u32 %9, %9, %21;\n\t"
+            "addc.cc.u32 %10, %10, %22;\n\t"
+            "addc.u32    %11, %11, %23;"
+            : "+r"(o[0]), "+r"(o[1]), "+r"(o[2]), "+r"(o[3]), "+r"(o[4]), "+r"(o[5]),
+              "+r"(o[6]), "+r"(o[7]), "+r"(o[8]), "+r"(o[9]), "+r"(o[10]), "+r"(o[11])
+            : "r"(e[1]), "r"(e[2]), "r"(e[3]), "r"(e[4]), "r"(e[5]), "r"(e[6]),
+              "r"(e[7]), "r"(e[8]), "r"(e[9]), "r"(e[10]), "r"(e[11]), "r"(e[12]));
+#pragma unroll
+        for (int k = 0; k < 12; k++) t[k] = o[k];
+    }
+    {   // step 9
+        const uint32_t bi = a.v[9];
+#pragma unroll
+        for (int k = 0; k < 12; k++) e[k] = t[k];
+        asm("mad.lo.cc.u32  %0, %3, %4, %0;\n\t"
+            "madc.hi.cc.u32 %1, %3, %4, %1;\n\t"
+            "addc.u32       %2, 0, 0;"
+            : "+r"(e[10]), "+r"(e[11]), "=r"(e[12])
+            : "r"((a.v[10] << 1)), "r"(bi));
+#pragma unroll
+        for (int k = 0; k < 13; k++) o[k] = 0;
+        o[8] = a.v[9] * bi;
+        o[9] = __umulhi(a.v[9], bi);
+        o[10] = d[11] * bi;
+        o[11] = __umulhi(d[11], bi);
+        const uint32_t m = e[0] * CATMSM_N0;
+        asm("mad.lo.cc.u32  %0, %13, %14, %0;\n\t"
+            "madc.hi.cc.u32 %1, %13, %14, %1;\n\t"
+            "madc.lo.cc.u32 %2, %13, %15, %2;\n\t"
+            "madc.hi.cc.u32 %3, %13, %15, %3;\n\t"
+            "madc.lo.cc.u32 %4, %13, %16, %4;\n\t"
+            "madc.hi.cc.u32 %5, %13, %16, %5;\n\t"
+            "madc.lo.cc.u32 %6, %13, %17, %6;\n\t"
+            "madc.hi.cc.u32 %7, %13, %17, %7;\n\t"
+            "madc.lo.cc.u32 %8, %13, %18, %8;\n\t"
+            "madc.hi.cc.u32 %9, %13, %18, %9;\n\t"
+            "madc.lo.cc.u32 %10, %13, %19, %10;\n\t"
+            "madc.hi.cc.u32 %11, %13, %19, %11;\n\t"
+            "addc.u32       %12, %12, 0;"
+            : "+r"(e[0]), "+r"(e[1]), "+r"(e[2]), "+r"(e[3]), "+r"(e[4]), "+r"(e[5]),
+              "+r"(e[6]), "+r"(e[7]), "+r"(e[8]), "+r"(e[9]), "+r"(e[10]), "+r"(e[11]),
+              "+r"(e[12])
+            : "r"(m), "n"(CATMSM_P0), "n"(CATMSM_P2), "n"(CATMSM_P4), "n"(CATMSM_P6),
+              "n"(CATMSM_P8), "n"(CATMSM_P10));
+        asm("mad.lo.cc.u32  %0, %13, %14, %0;\n\t"
+            "madc.hi.cc.u32 %1, %13, %14, %1;\n\t"
+            "madc.lo.cc.u32 %2, %13, %15, %2;\n\t"
+            "madc.hi.cc.u32 %3, %13, %15, %3;\n\t"
+            "madc.lo.cc.u32 %4, %13, %16, %4;\n\t"
+            "madc.hi.cc.u32 %5, %13, %16, %5;\n\t"
+            "madc.lo.cc.u32 %6, %13, %17, %6;\n\t"
+            "madc.hi.cc.u32 %7, %13, %17, %7;\n\t"
+            "madc.lo.cc.u32 %8, %13, %18, %8;\n\t"
+            "madc.hi.cc.u32 %9, %13, %18, %9;\n\t"
+            "madc.lo.cc.u32 %10, %13, %19, %10;\n\t"
+            "madc.hi.cc.u32 %11, %13, %19, %11;\n\t"
+            "addc.u32       %12, 0, 0;"
+            : "+r"(o[0]), "+r"(o[1]), "+r"(o[2]), "+r"(o[3]), "+r"(o[4]), "+r"(o[5]),
+              "+r"(o[6]), "+r"(o[7]), "+r"(o[8]), "+r"(o[9]), "+r"(o[10]), "+r"(o[11]),
+              "=r"(o[12])
+            : "r"(m), "n"(CATMSM_P1), "n"(CATMSM_P3), "n"(CATMSM_P5), "n"(CATMSM_P7),
+              "n"(CATMSM_P9), "n"(CATMSM_P11));
+        asm("add.cc.u32  %0, %0, %12;\n\t"
+            "addc.cc.u32 %1, %1, %13;\n\t"
+            "addc.cc.u32 %2, %2, %14;\n\t"
+            "addc.cc.u32 %3, %3, %15;\n\t"
+            "addc.cc.u32 %4, %4, %16;\n\t"
+            "addc.cc.u32 %5, %5, %17;\n\t"
+            "addc.cc.u32 %6, %6, %18;\n\t"
+            "addc.cc.u32 %7, %7, %19;\n\t"
+            "addc.cc.u32 %8, %8, %20;\n\t"
+            "addc.cc.u32 %9, %9, %21;\n\t"
+            "addc.cc.u32 %10, %10, %22;\n\t"
+            "addc.u32    %11, %11, %23;"
+            : "+r"(o[0]), "+r"(o[1]), "+r"(o[2]), "+r"(o[3]), "+r"(o[4]), "+r"(o[5]),
+              "+r"(o[6]), "+r"(o[7]), "+r"(o[8]), "+r"(o[9]), "+r"(o[10]), "+r"(o[11])
+            : "r"(e[1]), "r"(e[2]), "r"(e[3]), "r"(e[4]), "r"(e[5]), "r"(e[6]),
+              "r"(e[7]), "r"(e[8]), "r"(e[9]), "r"(e[10]), "r"(e[11]), "r"(e[12]));
+#pragma unroll
+        for (int k = 0; k < 12; k++) t[k] = o[k];
+    }
+    {   // step 10
+        const uint32_t bi = a.v[10];
+#pragma unroll
+        for (int k = 0; k < 12; k++) e[k] = t[k];
+        asm("mad.lo.cc.u32  %0, %3, %4, %0;\n\t"
+            "madc.hi.cc.u32 %1, %3, %4, %1;\n\t"
+            "addc.u32       %2, 0, 0;"
+            : "+r"(e[10]), "+r"(e[11]), "=r"(e[12])
+            : "r"(a.v[10]), "r"(bi));
+#pragma unroll
+        for (int k = 0; k < 13; k++) o[k] = 0;
+        o[10] = (a.v[11] << 1) * bi;
+        o[11] = __umulhi((a.v[11] << 1), bi);
+        const uint32_t m = e[0] * CATMSM_N0;
+        asm("mad.lo.cc.u32  %0, %13, %14, %0;\n\t"
+            "madc.hi.cc.u32 %1, %13, %14, %1;\n\t"
+            "madc.lo.cc.u32 %2, %13, %15, %2;\n\t"
+            "madc.hi.cc.u32 %3, %13, %15, %3;\n\t"
+            "madc.lo.cc.u32 %4, %13, %16, %4;\n\t"
+            "madc.hi.cc.u32 %5, %13, %16, %5;\n\t"
+            "madc.lo.cc.u32 %6, %13, %17, %6;\n\t"
+            "madc.hi.cc.u32 %7, %13, %17, %7;\n\t"
+            "madc.lo.cc.u32 %8, %13, %18, %8;\n\t"
+            "madc.hi.cc.u32 %9, %13, %18, %9;\n\t"
+            "madc.lo.cc.u32 %10, %13, %19, %10;\n\t"
+            "madc.hi.cc.u32 %11, %13, %19, %11;\n\t"
+            "addc.u32       %12, %12, 0;"
+            : "+r"(e[0]), "+r"(e[1]), "+r"(e[2]), "+r"(e[3]), "+r"(e[4]), "+r"(e[5]),
+              "+r"(e[6]), "+r"(e[7]), "+r"(e[8]), "+r"(e[9]), "+r"(e[10]), "+r"(e[11]),
+              "+r"(e[12])
+            : "r"(m), "n"(CATMSM_P0), "n"(CATMSM_P2), "n"(CATMSM_P4), "n"(CATMSM_P6),
+              "n"(CATMSM_P8), "n"(CATMSM_P10));
+        asm("mad.lo.cc.u32  %0, %13, %14, %0;\n\t"
+            "madc.hi.cc.u32 %1, %13, %14, %1;\n\t"
+            "madc.lo.cc.u32 %2, %13, %15, %2;\n\t"
+            "madc.hi.cc.u32 %3, %13, %15, %3;\n\t"
+            "madc.lo.cc.u32 %4, %13, %16, %4;\n\t"
+            "madc.hi.cc.u32 %5, %13, %16, %5;\n\t"
+            "madc.lo.cc.u32 %6, %13, %17, %6;\n\t"
+            "madc.hi.cc.u32 %7, %13, %17, %7;\n\t"
+            "madc.lo.cc.u32 %8, %13, %18, %8;\n\t"
+            "madc.hi.cc.u32 %9, %13, %18, %9;\n\t"
+            "madc.lo.cc.u32 %10, %13, %19, %10;\n\t"
+            "madc.hi.cc.u32 %11, %13, %19, %11;\n\t"
+            "addc.u32       %12, 0, 0;"
+            : "+r"(o[0]), "+r"(o[1]), "+r"(o[2]), "+r"(o[3]), "+r"(o[4]), "+r"(o[5]),
+              "+r"(o[6]), "+r"(o[7]), "+r"(o[8]), "+r"(o[9]), "+r"(o[10]), "+r"(o[11]),
+              "=r"(o[12])
+            : "r"(m), "n"(CATMSM_P1), "n"(CATMSM_P3), "n"(CATMSM_P5), "n"(CATMSM_P7),
+              "n"(CATMSM_P9), "n"(CATMSM_P11));
+        asm("add.cc.u32  %0, %0, %12;\n\t"
+            "addc.cc.u32 %1, %1, %13;\n\t"
+            "addc.cc.u32 %2, %2, %14;\n\t"
+            "addc.cc.u32 %3, %3, %15;\n\t"
+            "addc.cc.u32 %4, %4, %16;\n\t"
+            "addc.cc.u32 %5, %5, %17;\n\t"
+            "addc.cc.u32 %6, %6, %18;\n\t"
+            "addc.cc.u32 %7, %7, %19;\n\t"
+            "addc.cc.u32 %8, %8, %20;\n\t"
+            "addc.cc.u32 %9, %9, %21;\n\t"
+            "addc.cc.u32 %10, %10, %22;\n\t"
+            "addc.u32    %11, %11, %23;"
+            : "+r"(o[0]), "+r"(o[1]), "+r"(o[2]), "+r"(o[3]), "+r"(o[4]), "+r"(o[5]),
+              "+r"(o[6]), "+r"(o[7]), "+r"(o[8]), "+r"(o[9]), "+r"(o[10]), "+r"(o[11])
+            : "r"(e[1]), "r"(e[2]), "r"(e[3]), "r"(e[4]), "r"(e[5]), "r"(e[6]),
+              "r"(e[7]), "r"(e[8]), "r"(e[9]), "r"(e[10]), "r"(e[11]), "r"(e[12]));
+#pragma unroll
+        for (int k = 0; k < 12; k++) t[k] = o[k];
+    }
+    {   // step 11
+        const uint32_t bi = a.v[11];
+#pragma unroll
+        for (int k = 0; k < 12; k++) e[k] = t[k];
+        e[12] = 0;
+#pragma unroll
+        for (int k = 0; k < 13; k++) o[k] = 0;
+        o[10] = a.v[11] * bi;
+        o[11] = __umulhi(a.v[11], bi);
+        const uint32_t m = e[0] * CATMSM_N0;
+        asm("mad.lo.cc.u32  %0, %13, %14, %0;\n\t"
+            "madc.hi.cc.u32 %1, %13, %14, %1;\n\t"
+            "madc.lo.cc.u32 %2, %13, %15, %2;\n\t"
+            "madc.hi.cc.u32 %3, %13, %15, %3;\n\t"
+            "madc.lo.cc.u32 %4, %13, %16, %4;\n\t"
+            "madc.hi.cc.u32 %5, %13, %16, %5;\n\t"
+            "madc.lo.cc.u32 %6, %13, %17, %6;\n\t"
+            "madc.hi.cc.u32 %7, %13, %17, %7;\n\t"
+            "madc.lo.cc.u32 %8, %13, %18, %8;\n\t"
+            "madc.hi.cc.u32 %9, %13, %18, %9;\n\t"
+            "madc.lo.cc.u32 %10, %13, %19, %10;\n\t"
+            "madc.hi.cc.u32 %11, %13, %19, %11;\n\t"
+            "addc.u32       %12, %12, 0;"
+            : "+r"(e[0]), "+r"(e[1]), "+r"(e[2]), "+r"(e[3]), "+r"(e[4]), "+r"(e[5]),
+              "+r"(e[6]), "+r"(e[7]), "+r"(e[8]), "+r"(e[9]), "+r"(e[10]), "+r"(e[11]),
+              "+r"(e[12])
+            : "r"(m), "n"(CATMSM_P0), "n"(CATMSM_P2), "n"(CATMSM_P4), "n"(CATMSM_P6),
+              "n"(CATMSM_P8), "n"(CATMSM_P10));
+        asm("mad.lo.cc.u32  %0, %13, %14, %0;\n\t"
+            "madc.hi.cc.u32 %1, %13, %14, %1;\n\t"
+            "madc.lo.cc.u32 %2, %13, %15, %2;\n\t"
+            "madc.hi.cc.u32 %3, %13, %15, %3;\n\t"
+            "madc.lo.cc.u32 %4, %13, %16, %4;\n\t"
+            "madc.hi.cc.u32 %5, %13, %16, %5;\n\t"
+            "madc.lo.cc.u32 %6, %13, %17, %6;\n\t"
+            "madc.hi.cc.u32 %7, %13, %17, %7;\n\t"
+            "madc.lo.cc.u32 %8, %13, %18, %8;\n\t"
+            "madc.hi.cc.u32 %9, %13, %18, %9;\n\t"
+            "madc.lo.cc.u32 %10, %13, %19, %10;\n\t"
+            "madc.hi.cc.u32 %11, %13, %19, %11;\n\t"
+            "addc.u32       %12, 0, 0;"
+            : "+r"(o[0]), "+r"(o[1]), "+r"(o[2]), "+r"(o[3]), "+r"(o[4]), "+r"(o[5]),
+              "+r"(o[6]), "+r"(o[7]), "+r"(o[8]), "+r"(o[9]), "+r"(o[10]), "+r"(o[11]),
+              "=r"(o[12])
+            : "r"(m), "n"(CATMSM_P1), "n"(CATMSM_P3), "n"(CATMSM_P5), "n"(CATMSM_P7),
+              "n"(CATMSM_P9), "n"(CATMSM_P11));
+        asm("add.cc.u32  %0, %0, %12;\n\t"
+            "addc.cc.u32 %1, %1, %13;\n\t"
+            "addc.cc.u32 %2, %2, %14;\n\t"
+            "addc.cc.u32 %3, %3, %15;\n\t"
+            "addc.cc.u32 %4, %4, %16;\n\t"
+            "addc.cc.u32 %5, %5, %17;\n\t"
+            "addc.cc.u32 %6, %6, %18;\n\t"
+            "addc.cc.u32 %7, %7, %19;\n\t"
+            "addc.cc.u32 %8, %8, %20;\n\t"
+            "addc.cc.u32 %9, %9, %21;\n\t"
+            "addc.cc.u32 %10, %10, %22;\n\t"
+            "addc.u32    %11, %11, %23;"
+            : "+r"(o[0]), "+r"(o[1]), "+r"(o[2]), "+r"(o[3]), "+r"(o[4]), "+r"(o[5]),
+              "+r"(o[6]), "+r"(o[7]), "+r"(o[8]), "+r"(o[9]), "+r"(o[10]), "+r"(o[11])
+            : "r"(e[1]), "r"(e[2]), "r"(e[3]), "r"(e[4]), "r"(e[5]), "r"(e[6]),
+              "r"(e[7]), "r"(e[8]), "r"(e[9]), "r"(e[10]), "r"(e[11]), "r"(e[12]));
+#pragma unroll
+        for (int k = 0; k < 12; k++) t[k] = o[k];
+    }
+#pragma unroll
+    for (int k = 0; k < 12; k++) r.v[k] = t[k];
+}
+
+static __device__ __noinline__ fp fp_sqr_call(const fp a)
+{
+    fp r;
+    fp_sqr_impl(r, a);
+    return r;
+}
+
+__device__ __forceinline__ void fp_sqr(fp& r, const fp& a) { r = fp_sqr_call(a); }
 
 // r = a + b mod 2p (inputs < 2p)
 __device__ __forceinline__ void fp_add(fp& r, const fp& a, const fp& b)
