@@ -49,9 +49,8 @@ __device__ __forceinline__ void xyzz_dbl_affine(xyzz& p, const fp& ax, const fp&
     fp_sub(t, t, S);
     fp_sub(p.x, t, S);
     fp_sub(t, S, p.x);
-    fp_mul(t, M, t);
-    fp_mul(S, W, ay);
-    fp_sub(p.y, t, S);
+    fp_neg(S, ay);
+    fp_mul2(p.y, M, t, W, S);     // Y3 = M (S - X3) - W y, one reduction
     p.zz = V;
     p.zzz = W;
 }
@@ -85,9 +84,8 @@ __device__ __forceinline__ void xyzz_madd(xyzz& p, const fp& ax, const fp& ay)
     fp_sub(P, P, Q);
     fp_sub(p.x, P, Q);            // X3 = R^2 - PPP - 2Q
     fp_sub(Q, Q, p.x);
-    fp_mul(Q, Q, R);              // R (Q - X3)
-    fp_mul(PPP, p.y, PPP);        // Y1 PPP
-    fp_sub(p.y, Q, PPP);
+    fp_neg(PPP, PPP);
+    fp_mul2(p.y, Q, R, p.y, PPP); // Y3 = R (Q - X3) - Y1 PPP, one reduction
 }
 
 // p = 2p (dbl-2008-s)
@@ -108,9 +106,8 @@ __device__ __forceinline__ void xyzz_dbl(xyzz& p)
     fp_sub(t, t, S);
     fp_sub(p.x, t, S);
     fp_sub(t, S, p.x);
-    fp_mul(t, M, t);
-    fp_mul(W, W, p.y);
-    fp_sub(p.y, t, W);
+    fp_neg(W, W);
+    fp_mul2(p.y, M, t, W, p.y);   // Y3 = M (S - X3) - W Y1, one reduction
 }
 
 // p += q (add-2008-s, 12M + 2S)
@@ -143,9 +140,8 @@ __device__ __forceinline__ void xyzz_add(xyzz& p, const xyzz& q)
     fp_sub(P, P, U1);
     fp_sub(p.x, P, U1);
     fp_sub(U1, U1, p.x);
-    fp_mul(U1, U1, R);
-    fp_mul(S1, S1, PPP);
-    fp_sub(p.y, U1, S1);
+    fp_neg(PPP, PPP);
+    fp_mul2(p.y, U1, R, S1, PPP); // Y3 = R (Q - X3) - S1 PPP, one reduction
 }
 
 __device__ __forceinline__ void xyzz_neg(xyzz& p) { fp_neg(p.y, p.y); }
@@ -248,14 +244,13 @@ __device__ __forceinline__ void jac_add(jac& p, const jac& q)
     fp_sqr(t, h);                 // HH
     fp_mul(u1, u1, t);            // V = U1 HH
     fp_mul(t, t, h);              // HHH
-    fp_mul(s1, s1, t);            // S1 HHH
     fp_sqr(z1z1, r);
     fp_sub(z1z1, z1z1, t);
     fp_sub(z1z1, z1z1, u1);
     fp_sub(p.x, z1z1, u1);        // X3 = R^2 - HHH - 2V
     fp_sub(u1, u1, p.x);
-    fp_mul(u1, u1, r);
-    fp_sub(p.y, u1, s1);          // Y3 = R (V - X3) - S1 HHH
+    fp_neg(t, t);
+    fp_mul2(p.y, u1, r, s1, t);   // Y3 = R (V - X3) - S1 HHH, one reduction
 }
 
 __device__ __forceinline__ void jac_neg(jac& p) { fp_neg(p.y, p.y); }

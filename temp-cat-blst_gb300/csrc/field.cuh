@@ -1131,6 +1131,146 @@ static __device__ __noinline__ fp fp_sqr_call(const fp a)
 
 __device__ __forceinline__ void fp_sqr(fp& r, const fp& a) { r = fp_sqr_call(a); }
 
+// r = (a * b + c * d) * 2^-384 mod p; inputs in [0, 2p), output in [0, 2p).
+// The CIOS schedule of fp_mul_impl with both products added in each step
+// before its single Montgomery reduction (876 IMAD against 2 x 588).  Each
+// step adds at most 4p 2^32, so the running value stays below 6p < 2^384,
+// and a b + c d < 8p^2 < p 2^384 leaves the result below 1.82p.
+__device__ __forceinline__ void fp_mul2_impl(fp& r, const fp& a, const fp& b, const fp& c, const fp& d)
+{
+    uint32_t t[12], e[13], o[13];
+#pragma unroll
+    for (int i = 0; i < 12; i++) {
+        const uint32_t bi = b.v[i], di = d.v[i];
+        if (i == 0) {
+#pragma unroll
+            for (int k = 0; k < 6; k++) {
+                e[2 * k] = a.v[2 * k] * bi;
+                e[2 * k + 1] = __umulhi(a.v[2 * k], bi);
+            }
+            e[12] = 0;
+        } else {
+#pragma unroll
+            for (int k = 0; k < 12; k++) e[k] = t[k];
+            asm("mad.lo.cc.u32  %0, %13, %14, %0;\n\t"
+                "madc.hi.cc.u32 %1, %13, %14, %1;\n\t"
+                "madc.lo.cc.u32 %2, %13, %15, %2;\n\t"
+                "madc.hi.cc.u32 %3, %13, %15, %3;\n\t"
+                "madc.lo.cc.u32 %4, %13, %16, %4;\n\t"
+                "madc.hi.cc.u32 %5, %13, %16, %5;\n\t"
+                "madc.lo.cc.u32 %6, %13, %17, %6;\n\t"
+                "madc.hi.cc.u32 %7, %13, %17, %7;\n\t"
+                "madc.lo.cc.u32 %8, %13, %18, %8;\n\t"
+                "madc.hi.cc.u32 %9, %13, %18, %9;\n\t"
+                "madc.lo.cc.u32 %10, %13, %19, %10;\n\t"
+                "madc.hi.cc.u32 %11, %13, %19, %11;\n\t"
+                "addc.u32       %12, 0, 0;"
+                : "+r"(e[0]), "+r"(e[1]), "+r"(e[2]), "+r"(e[3]), "+r"(e[4]), "+r"(e[5]), "+r"(e[6]), "+r"(e[7]), "+r"(e[8]), "+r"(e[9]), "+r"(e[10]), "+r"(e[11]), "=r"(e[12])
+                : "r"(bi), "r"(a.v[0]), "r"(a.v[2]), "r"(a.v[4]), "r"(a.v[6]), "r"(a.v[8]), "r"(a.v[10]));
+        }
+        asm("mad.lo.cc.u32  %0, %13, %14, %0;\n\t"
+            "madc.hi.cc.u32 %1, %13, %14, %1;\n\t"
+            "madc.lo.cc.u32 %2, %13, %15, %2;\n\t"
+            "madc.hi.cc.u32 %3, %13, %15, %3;\n\t"
+            "madc.lo.cc.u32 %4, %13, %16, %4;\n\t"
+            "madc.hi.cc.u32 %5, %13, %16, %5;\n\t"
+            "madc.lo.cc.u32 %6, %13, %17, %6;\n\t"
+            "madc.hi.cc.u32 %7, %13, %17, %7;\n\t"
+            "madc.lo.cc.u32 %8, %13, %18, %8;\n\t"
+            "madc.hi.cc.u32 %9, %13, %18, %9;\n\t"
+            "madc.lo.cc.u32 %10, %13, %19, %10;\n\t"
+            "madc.hi.cc.u32 %11, %13, %19, %11;\n\t"
+            "addc.u32       %12, %12, 0;"
+            : "+r"(e[0]), "+r"(e[1]), "+r"(e[2]), "+r"(e[3]), "+r"(e[4]), "+r"(e[5]), "+r"(e[6]), "+r"(e[7]), "+r"(e[8]), "+r"(e[9]), "+r"(e[10]), "+r"(e[11]), "+r"(e[12])
+            : "r"(di), "r"(c.v[0]), "r"(c.v[2]), "r"(c.v[4]), "r"(c.v[6]), "r"(c.v[8]), "r"(c.v[10]));
+#pragma unroll
+        for (int k = 0; k < 6; k++) {
+            o[2 * k] = a.v[2 * k + 1] * bi;
+            o[2 * k + 1] = __umulhi(a.v[2 * k + 1], bi);
+        }
+        asm("mad.lo.cc.u32  %0, %13, %14, %0;\n\t"
+            "madc.hi.cc.u32 %1, %13, %14, %1;\n\t"
+            "madc.lo.cc.u32 %2, %13, %15, %2;\n\t"
+            "madc.hi.cc.u32 %3, %13, %15, %3;\n\t"
+            "madc.lo.cc.u32 %4, %13, %16, %4;\n\t"
+            "madc.hi.cc.u32 %5, %13, %16, %5;\n\t"
+            "madc.lo.cc.u32 %6, %13, %17, %6;\n\t"
+            "madc.hi.cc.u32 %7, %13, %17, %7;\n\t"
+            "madc.lo.cc.u32 %8, %13, %18, %8;\n\t"
+            "madc.hi.cc.u32 %9, %13, %18, %9;\n\t"
+            "madc.lo.cc.u32 %10, %13, %19, %10;\n\t"
+            "madc.hi.cc.u32 %11, %13, %19, %11;\n\t"
+            "addc.u32       %12, 0, 0;"
+            : "+r"(o[0]), "+r"(o[1]), "+r"(o[2]), "+r"(o[3]), "+r"(o[4]), "+r"(o[5]), "+r"(o[6]), "+r"(o[7]), "+r"(o[8]), "+r"(o[9]), "+r"(o[10]), "+r"(o[11]), "=r"(o[12])
+            : "r"(di), "r"(c.v[1]), "r"(c.v[3]), "r"(c.v[5]), "r"(c.v[7]), "r"(c.v[9]), "r"(c.v[11]));
+        const uint32_t m = e[0] * CATMSM_N0;
+        asm("mad.lo.cc.u32  %0, %13, %14, %0;\n\t"
+            "madc.hi.cc.u32 %1, %13, %14, %1;\n\t"
+            "madc.lo.cc.u32 %2, %13, %15, %2;\n\t"
+            "madc.hi.cc.u32 %3, %13, %15, %3;\n\t"
+            "madc.lo.cc.u32 %4, %13, %16, %4;\n\t"
+            "madc.hi.cc.u32 %5, %13, %16, %5;\n\t"
+            "madc.lo.cc.u32 %6, %13, %17, %6;\n\t"
+            "madc.hi.cc.u32 %7, %13, %17, %7;\n\t"
+            "madc.lo.cc.u32 %8, %13, %18, %8;\n\t"
+            "madc.hi.cc.u32 %9, %13, %18, %9;\n\t"
+            "madc.lo.cc.u32 %10, %13, %19, %10;\n\t"
+            "madc.hi.cc.u32 %11, %13, %19, %11;\n\t"
+            "addc.u32       %12, %12, 0;"
+            : "+r"(e[0]), "+r"(e[1]), "+r"(e[2]), "+r"(e[3]), "+r"(e[4]), "+r"(e[5]), "+r"(e[6]), "+r"(e[7]), "+r"(e[8]), "+r"(e[9]), "+r"(e[10]), "+r"(e[11]), "+r"(e[12])
+            : "r"(m), "n"(CATMSM_P0), "n"(CATMSM_P2), "n"(CATMSM_P4), "n"(CATMSM_P6), "n"(CATMSM_P8), "n"(CATMSM_P10));
+        asm("mad.lo.cc.u32  %0, %13, %14, %0;\n\t"
+            "madc.hi.cc.u32 %1, %13, %14, %1;\n\t"
+            "madc.lo.cc.u32 %2, %13, %15, %2;\n\t"
+            "madc.hi.cc.u32 %3, %13, %15, %3;\n\t"
+            "madc.lo.cc.u32 %4, %13, %16, %4;\n\t"
+            "madc.hi.cc.u32 %5, %13, %16, %5;\n\t"
+            "madc.lo.cc.u32 %6, %13, %17, %6;\n\t"
+            "madc.hi.cc.u32 %7, %13, %17, %7;\n\t"
+            "madc.lo.cc.u32 %8, %13, %18, %8;\n\t"
+            "madc.hi.cc.u32 %9, %13, %18, %9;\n\t"
+            "madc.lo.cc.u32 %10, %13, %19, %10;\n\t"
+            "madc.hi.cc.u32 %11, %13, %19, %11;\n\t"
+            "addc.u32       %12, %12, 0;"
+            : "+r"(o[0]), "+r"(o[1]), "+r"(o[2]), "+r"(o[3]), "+r"(o[4]), "+r"(o[5]), "+r"(o[6]), "+r"(o[7]), "+r"(o[8]), "+r"(o[9]), "+r"(o[10]), "+r"(o[11]), "+r"(o[12])
+            : "r"(m), "n"(CATMSM_P1), "n"(CATMSM_P3), "n"(CATMSM_P5), "n"(CATMSM_P7), "n"(CATMSM_P9), "n"(CATMSM_P11));
+        // t = (E + O*2^32) / 2^32 (the weight-13 word is zero by the bound)
+        asm("add.cc.u32  %0, %0, %12;\n\t"
+            "addc.cc.u32 %1, %1, %13;\n\t"
+            "addc.cc.u32 %2, %2, %14;\n\t"
+            "addc.cc.u32 %3, %3, %15;\n\t"
+            "addc.cc.u32 %4, %4, %16;\n\t"
+            "addc.cc.u32 %5, %5, %17;\n\t"
+            "addc.cc.u32 %6, %6, %18;\n\t"
+            "addc.cc.u32 %7, %7, %19;\n\t"
+            "addc.cc.u32 %8, %8, %20;\n\t"
+            "addc.cc.u32 %9, %9, %21;\n\t"
+            "addc.cc.u32 %10, %10, %22;\n\t"
+            "addc.u32    %11, %11, %23;"
+            : "+r"(o[0]), "+r"(o[1]), "+r"(o[2]), "+r"(o[3]), "+r"(o[4]), "+r"(o[5]),
+              "+r"(o[6]), "+r"(o[7]), "+r"(o[8]), "+r"(o[9]), "+r"(o[10]), "+r"(o[11])
+            : "r"(e[1]), "r"(e[2]), "r"(e[3]), "r"(e[4]), "r"(e[5]), "r"(e[6]),
+              "r"(e[7]), "r"(e[8]), "r"(e[9]), "r"(e[10]), "r"(e[11]), "r"(e[12]));
+#pragma unroll
+        for (int k = 0; k < 12; k++) t[k] = o[k];
+    }
+#pragma unroll
+    for (int k = 0; k < 12; k++) r.v[k] = t[k];
+}
+
+static __device__ __noinline__ fp fp_mul2_call(const fp a, const fp b, const fp c, const fp d)
+{
+    fp r;
+    fp_mul2_impl(r, a, b, c, d);
+    return r;
+}
+
+// r = a * b + c * d (Montgomery), one reduction
+__device__ __forceinline__ void fp_mul2(fp& r, const fp& a, const fp& b, const fp& c, const fp& d)
+{
+    r = fp_mul2_call(a, b, c, d);
+}
+
 // r = a + b mod 2p (inputs < 2p)
 __device__ __forceinline__ void fp_add(fp& r, const fp& a, const fp& b)
 {
