@@ -323,6 +323,11 @@ static void enqueue_batch(const Basis* b, BatchWork* w, cudaStream_t st, uint32_
     uint32_t m = B, pp = 0;
     bool first = true;
     while (m > 1) {
+        if (!first && m <= msm_reduce_tail_max()) {
+            msm_reduce_tail(inA, inQ, m, nmsm, bufQ[pp], st);
+            inQ = bufQ[pp];
+            break;
+        }
         const uint32_t F = first ? 8 : 2, lgF = first ? 3 : 1;
         const uint32_t m_out = (m + F - 1) / F;
         k_reduce_level<<<div_up((size_t)nmsm * m_out, 128), 128, 0, st>>>(inA, inQ, m, F, lgF, nmsm, first ? 1 : 0,
@@ -480,7 +485,7 @@ void* catmsm_basis_create(const blst_p1_affine* points, size_t n, size_t window)
     if (!points || n == 0 || n > (1u << 24) || window > 20 || (window != 0 && window < 2)) return nullptr;
     Basis* b = new (std::nothrow) Basis();
     if (!b) return nullptr;
-    if (cudaGetDevice(&b->device) != cudaSuccess ||
+    if (cudaGetDevice(&b->device) != cudaSuccess || msm_setup_device() != cudaSuccess ||
         cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) {
         delete b;
         return nullptr;

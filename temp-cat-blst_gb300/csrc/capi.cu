@@ -30,6 +30,11 @@ Ctx* get_ctx()
             delete c;
             return nullptr;
         }
+        if (msm_setup_device() != cudaSuccess) {
+            cudaStreamDestroy(c->stream);
+            delete c;
+            return nullptr;
+        }
         per_dev[dev] = c;
     }
     return per_dev[dev];

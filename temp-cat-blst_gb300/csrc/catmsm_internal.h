@@ -25,6 +25,15 @@ int basis_device(const Basis* b);
 // the GLV split applies).
 void msm_plan(const Ctx* ctx, size_t n, uint32_t nbits, uint32_t* c, uint32_t* windows, size_t* points);
 
+// Per-device set-up of the MSM kernels (shared-memory limits), run once per
+// context.
+cudaError_t msm_setup_device();
+
+// The fused last reduction levels for D independent sets of m (A, Q) XYZZ
+// pairs (m <= msm_reduce_tail_max()); roots to outQ[0..D).
+uint32_t msm_reduce_tail_max();
+void msm_reduce_tail(const void* inA, const void* inQ, uint32_t m, uint32_t D, void* outQ, cudaStream_t st);
+
 cudaError_t msm_device(Ctx* ctx, const void* d_points, const uint8_t* d_scalars, uint32_t stride,
                        size_t n, uint32_t nbits, uint32_t c, uint64_t* out);
 

@@ -490,6 +490,66 @@ __global__ void __launch_bounds__(128) k_reduce_level(const xyzz* __restrict__ i
     store_xyzz(outQ + (size_t)w * m_out + u, tt);
 }
 
+// The last binary levels in one launch: block w reduces window w's m_in
+// (A, Q) pairs (m_in <= 2 kTailThreads) to its root Q in shared memory with
+// one barrier per level, instead of one launch and a global round trip per
+// level (each upper level is a ~2-operation dependent chain, so launch gaps
+// and memory latency dominated them).  A node's rule is k_reduce_level's
+// with fan-in 2: Q = A_1 + Q_0 + Q_1, A = 2 (A_0 + A_1); a node with one
+// child keeps Q_0 and doubles A_0.
+constexpr int kTailThreads = 256;
+constexpr size_t kTailShared = 2 * kTailThreads * sizeof(xyzz);
+
+__device__ __forceinline__ void tail_node(xyzz& A, xyzz& Q, const xyzz* a, const xyzz* q, uint32_t cnt, bool need_a)
+{
+    xyzz b;
+    if (cnt == 2) {
+        load_xyzz(A, a + 1);
+        Q = A;
+        load_xyzz(b, q);
+        xyzz_add(Q, b);
+        load_xyzz(b, q + 1);
+        xyzz_add(Q, b);
+        if (need_a) {
+            load_xyzz(b, a);
+            xyzz_add(A, b);
+        }
+    } else {
+        load_xyzz(Q, q);
+        if (need_a) load_xyzz(A, a);
+    }
+    if (need_a) xyzz_dbl(A);
+}
+
+__global__ void __launch_bounds__(kTailThreads) k_reduce_tail(const xyzz* __restrict__ inA,
+                                                              const xyzz* __restrict__ inQ, uint32_t m_in,
+                                                              xyzz* __restrict__ outQ)
+{
+    extern __shared__ __align__(16) unsigned char tail_smem[];
+    xyzz* shA = reinterpret_cast<xyzz*>(tail_smem);
+    xyzz* shQ = shA + kTailThreads;
+    const uint32_t w = blockIdx.x, t = threadIdx.x;
+    uint32_t m = m_in;
+    const xyzz* srcA = inA + (size_t)w * m_in;
+    const xyzz* srcQ = inQ + (size_t)w * m_in;
+    while (m > 1) {
+        const uint32_t m_out = (m + 1) / 2;
+        xyzz A, Q;
+        const bool act = t < m_out;
+        if (act) tail_node(A, Q, srcA + 2 * t, srcQ + 2 * t, min(2u, m - 2 * t), m_out > 1);
+        __syncthreads();
+        if (act) {
+            shQ[t] = Q;
+            if (m_out > 1) shA[t] = A;
+        }
+        __syncthreads();
+        srcA = shA;
+        srcQ = shQ;
+        m = m_out;
+    }
+    if (t == 0) store_xyzz(outQ + w, m_in == 1 ? srcQ[0] : shQ[0]);
+}
+
 // ----------------------------------------------------------------- host driver
 static uint32_t ilog2(size_t n)
 {
@@ -525,6 +585,18 @@ uint32_t msm_glv_window(size_t n2)
         if (bc == 0 || cost < best) { best = cost; bc = c; }
     }
     return bc;
+}
+
+cudaError_t msm_setup_device()
+{
+    return cudaFuncSetAttribute(k_reduce_tail, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTailShared);
+}
+
+uint32_t msm_reduce_tail_max() { return 2 * kTailThreads; }
+
+void msm_reduce_tail(const void* inA, const void* inQ, uint32_t m, uint32_t D, void* outQ, cudaStream_t st)
+{
+    k_reduce_tail<<<D, kTailThreads, kTailShared, st>>>((const xyzz*)inA, (const xyzz*)inQ, m, (xyzz*)outQ);
 }
 
 static bool use_glv(const Ctx* ctx, size_t n, uint32_t nbits)
@@ -637,6 +709,13 @@ cudaError_t msm_device(Ctx* ctx, const void* d_points, const uint8_t* d_scalars,
         uint32_t m = B, pp = 0;
         bool first = true;
         while (m > 1) {
+            if (!first && m <= 2 * kTailThreads) {
+                k_reduce_tail<<<D, kTailThreads, kTailShared, st>>>(inA, inQ, m, bufQ[pp]);
+                g_stats.launches++;
+                inQ = bufQ[pp];
+                m = 1;
+                break;
+            }
             const uint32_t F = first ? S : 2, lgF = first ? 3 : 1;
             const uint32_t m_out = (m + F - 1) / F;
             k_reduce_level<<<div_up((size_t)D * m_out, 128), 128, 0, st>>>(inA, inQ, m, F, lgF, D, first ? 1 : 0,
