@@ -350,18 +350,23 @@ def p1s_affine_in_g1(points: bytes, n: int):
 
 def p1_fft_batch(values_list, ns, domains, modes):
     """Batch of G1 FFTs; returns (rc, list of output byte strings)."""
-    L = load()
     bufs = [bytearray(v) for v in values_list]
-    doms = [bytearray(d) for d in domains]
-    vb = [_buf(b) for b in bufs]
-    db = [_buf(d) for d in doms]
+    rc = p1_fft_batch_inplace(bufs, ns, domains, modes)
+    return rc, [bytes(b) for b in bufs]
+
+
+def p1_fft_batch_inplace(bufs, ns, domains, modes):
+    """Batch of G1 FFTs transforming the given bytearrays in place (domains:
+    bytes or bytearray, read only); returns the status code."""
+    L = load()
+    vb = [(C.c_char * len(b)).from_buffer(b) for b in bufs]
+    db = [(C.c_char * len(d)).from_buffer(d) if isinstance(d, bytearray) else C.c_char_p(bytes(d)) for d in domains]
     count = len(bufs)
     varr = (C.c_void_p * count)(*[C.cast(x, C.c_void_p) for x in vb])
     darr = (C.c_void_p * count)(*[C.cast(x, C.c_void_p) for x in db])
     narr = (C.c_size_t * count)(*ns)
     marr = (C.c_int * count)(*modes)
-    rc = L.catmsm_p1_fft_batch(varr, narr, darr, marr, count)
-    return rc, [bytes(b) for b in bufs]
+    return L.catmsm_p1_fft_batch(varr, narr, darr, marr, count)
 
 
 def points_from_scalars(k32: bytes, n: int) -> bytes:
@@ -486,23 +491,29 @@ class Basis:
             raise RuntimeError("catmsm_basis_set_config failed: %d" % rc)
 
     def _args(self, counts, scalars):
+        """counts as a size_t array; scalars as a pointer without copying:
+        bytes / bytearray (read in place) or an int host address (e.g. a
+        pinned buffer's data_ptr())."""
         cnt = (C.c_size_t * len(counts))(*counts)
-        sb = bytearray(scalars)
-        return cnt, sb
+        if isinstance(scalars, int):
+            return cnt, C.c_void_p(scalars)
+        if isinstance(scalars, bytearray):
+            return cnt, (C.c_char * len(scalars)).from_buffer(scalars)
+        return cnt, C.c_char_p(bytes(scalars))
 
     def msm_batch(self, counts, scalars: bytes, use_graph=True) -> bytes:
         """counts[j] points per MSM; scalars: concatenated 32-byte scalars.
         Returns len(counts) Jacobian blst_p1 (144 bytes each)."""
         cnt, sb = self._args(counts, scalars)
         out = bytearray(P1 * len(counts))
-        rc = self.L.catmsm_basis_msm_batch(self.h, _buf(out), len(counts), cnt, _buf(sb), 1 if use_graph else 0)
+        rc = self.L.catmsm_basis_msm_batch(self.h, _buf(out), len(counts), cnt, sb, 1 if use_graph else 0)
         if rc != 0:
             raise RuntimeError("catmsm_basis_msm_batch failed: %d" % rc)
         return bytes(out)
 
     def autotune(self, counts, scalars: bytes, force=False):
         cnt, sb = self._args(counts, scalars)
-        rc = self.L.catmsm_basis_autotune(self.h, len(counts), cnt, _buf(sb), 1 if force else 0)
+        rc = self.L.catmsm_basis_autotune(self.h, len(counts), cnt, sb, 1 if force else 0)
         if rc != 0:
             raise RuntimeError("catmsm_basis_autotune failed: %d" % rc)
         return self.config()

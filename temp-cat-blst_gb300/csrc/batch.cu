@@ -358,7 +358,7 @@ static cudaError_t run_batch(Basis* b, BatchWork* w, cudaStream_t st, blst_p1* o
     const size_t cap = exact_cap ? (P ? P : 1) : (size_t)nmsm * b->n;
     if (cap * b->D >= 0x7fffffffu) return cudaErrorInvalidValue;
     CATMSM_CHECK(ensure_work(b, w, nmsm, cap));
-    std::memcpy(w->h_scal.p, scalars, P * 32);
+    host_copy(w->h_scal.p, scalars, P * 32);
     std::memcpy(w->h_off.p, off.data(), (nmsm + 1) * 4);
     CATMSM_CHECK(cudaMemcpyAsync(w->scal.p, w->h_scal.p, P * 32, cudaMemcpyHostToDevice, st));
     CATMSM_CHECK(cudaMemcpyAsync(w->off.p, w->h_off.p, (nmsm + 1) * 4, cudaMemcpyHostToDevice, st));

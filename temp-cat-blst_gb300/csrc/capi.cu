@@ -141,7 +141,7 @@ static bool fft_entry(blst_p1* values, size_t n, const blst_fr* domain, bool inv
     if (err == cudaSuccess) err = cudaMemcpyAsync(hstage, dv, n * sizeof(blst_p1), cudaMemcpyDeviceToHost, st);
     if (err == cudaSuccess) err = cudaStreamSynchronize(st);
     if (err != cudaSuccess) return false;
-    std::memcpy(values, hstage, n * sizeof(blst_p1));
+    host_copy(values, hstage, n * sizeof(blst_p1));
     return true;
 }
 
@@ -306,7 +306,7 @@ int catmsm_p1_fft_batch(blst_p1* const values[], const size_t ns[], const blst_f
         if (err != cudaSuccess) return (int)err;
         off = 0;
         for (size_t i = 0; i < count; i++) {
-            std::memcpy(values[i], (const blst_p1*)hstage + off, ns[i] * sizeof(blst_p1));
+            host_copy(values[i], (const blst_p1*)hstage + off, ns[i] * sizeof(blst_p1));
             off += ns[i];
         }
         return 0;

@@ -205,7 +205,7 @@ static bool fr_fft_entry(blst_fr* values, size_t n, const blst_fr* domain, bool 
     if (err == cudaSuccess) err = cudaMemcpyAsync(hstage, dv, n * 32, cudaMemcpyDeviceToHost, st);
     if (err == cudaSuccess) err = cudaStreamSynchronize(st);
     if (err != cudaSuccess) return false;
-    std::memcpy(values, hstage, n * 32);
+    host_copy(values, hstage, n * 32);
     return true;
 }
 
