@@ -491,7 +491,9 @@ __global__ void __launch_bounds__(128) k_reduce_level(const xyzz* __restrict__ i
 }
 
 // The last binary levels in one launch: block w reduces window w's m_in
-// (A, Q) pairs (m_in <= 2 kTailThreads) to its root Q in shared memory with
+// (A, Q) pairs (m_in <= 2 blockDim.x, blockDim.x <= kTailThreads; the block
+// is sized to the first level's nodes so that many windows fit on an SM) to
+// its root Q in shared memory with
 // one barrier per level, instead of one launch and a global round trip per
 // level (each upper level is a ~2-operation dependent chain, so launch gaps
 // and memory latency dominated them).  A node's rule is k_reduce_level's
@@ -527,7 +529,7 @@ __global__ void __launch_bounds__(kTailThreads) k_reduce_tail(const xyzz* __rest
 {
     extern __shared__ __align__(16) unsigned char tail_smem[];
     xyzz* shA = reinterpret_cast<xyzz*>(tail_smem);
-    xyzz* shQ = shA + kTailThreads;
+    xyzz* shQ = shA + blockDim.x;
     const uint32_t w = blockIdx.x, t = threadIdx.x;
     uint32_t m = m_in;
     const xyzz* srcA = inA + (size_t)w * m_in;
@@ -596,7 +598,8 @@ uint32_t msm_reduce_tail_max() { return 2 * kTailThreads; }
 
 void msm_reduce_tail(const void* inA, const void* inQ, uint32_t m, uint32_t D, void* outQ, cudaStream_t st)
 {
-    k_reduce_tail<<<D, kTailThreads, kTailShared, st>>>((const xyzz*)inA, (const xyzz*)inQ, m, (xyzz*)outQ);
+    const uint32_t T = ((m + 1) / 2 + 31) / 32 * 32;   // m <= 2 kTailThreads
+    k_reduce_tail<<<D, T, 2 * T * sizeof(xyzz), st>>>((const xyzz*)inA, (const xyzz*)inQ, m, (xyzz*)outQ);
 }
 
 static bool use_glv(const Ctx* ctx, size_t n, uint32_t nbits)
@@ -710,7 +713,7 @@ cudaError_t msm_device(Ctx* ctx, const void* d_points, const uint8_t* d_scalars,
         bool first = true;
         while (m > 1) {
             if (!first && m <= 2 * kTailThreads) {
-                k_reduce_tail<<<D, kTailThreads, kTailShared, st>>>(inA, inQ, m, bufQ[pp]);
+                msm_reduce_tail(inA, inQ, m, D, bufQ[pp], st);
                 g_stats.launches++;
                 inQ = bufQ[pp];
                 m = 1;
