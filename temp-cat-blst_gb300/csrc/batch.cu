@@ -49,6 +49,15 @@ __global__ void k_fixup(const uint32_t* __restrict__ sorted_key, const uint32_t*
 __global__ void k_fixup_hot(const uint2* __restrict__ hot_list, const uint32_t* __restrict__ hot_count,
                             const uint32_t* __restrict__ offsets, uint32_t L, xyzz* __restrict__ buckets,
                             const xyzz* __restrict__ head, const xyzz* __restrict__ tail);
+__global__ void k_fixup_seg(const uint32_t* __restrict__ sorted_key, const uint32_t* __restrict__ total_ptr,
+                            uint32_t L, xyzz* __restrict__ head);
+__global__ void k_fixup_join(const uint32_t* __restrict__ sorted_key, const uint32_t* __restrict__ offsets,
+                             const uint32_t* __restrict__ total_ptr, uint32_t L, xyzz* __restrict__ buckets,
+                             const xyzz* __restrict__ head, const xyzz* __restrict__ tail,
+                             uint2* __restrict__ hot_list, uint32_t* __restrict__ hot_count);
+__global__ void k_fixup_hot_seg(const uint2* __restrict__ hot_list, const uint32_t* __restrict__ hot_count,
+                                const uint32_t* __restrict__ offsets, uint32_t L, xyzz* __restrict__ buckets,
+                                const xyzz* __restrict__ head, const xyzz* __restrict__ tail);
 __global__ void k_reduce_level(const xyzz* __restrict__ inA, const xyzz* __restrict__ inQ, uint32_t m_in,
                                uint32_t F, uint32_t lgF, uint32_t D, int first, xyzz* __restrict__ outA,
                                xyzz* __restrict__ outQ);
@@ -313,9 +322,10 @@ static void enqueue_batch(const Basis* b, BatchWork* w, cudaStream_t st, uint32_
     k_accumulate<<<div_up(chunks, 128), 128, 0, st>>>((const affine*)b->table.p, (const uint32_t*)w->sorted_pt.p,
                                                       (const uint32_t*)w->sorted_key.p, total, L, buckets, head,
                                                       tail);
-    k_fixup<<<div_up(chunks, 128), 128, 0, st>>>((const uint32_t*)w->sorted_key.p, offsets, total, L, buckets, head,
-                                                 tail, hot_list, hot_count);
-    k_fixup_hot<<<2 * kSMs, 128, 0, st>>>(hot_list, hot_count, offsets, L, buckets, head, tail);
+    k_fixup_seg<<<div_up(chunks, 128), 128, 0, st>>>((const uint32_t*)w->sorted_key.p, total, L, head);
+    k_fixup_join<<<div_up(chunks, 128), 128, 0, st>>>((const uint32_t*)w->sorted_key.p, offsets, total, L, buckets,
+                                                      head, tail, hot_list, hot_count);
+    k_fixup_hot_seg<<<2 * kSMs, 128, 0, st>>>(hot_list, hot_count, offsets, L, buckets, head, tail);
     xyzz* bufA[2] = {seg, seg + 2 * lvl1};
     xyzz* bufQ[2] = {seg + lvl1, seg + 2 * lvl1 + lvl2};
     const xyzz* inA = buckets;
@@ -383,7 +393,7 @@ static cudaError_t run_batch(Basis* b, BatchWork* w, cudaStream_t st, blst_p1* o
         g_stats.launches += 1;
     } else {
         enqueue_batch(b, w, st, nmsm, cap);
-        g_stats.launches += 12;
+        g_stats.launches += 13;
     }
     CATMSM_CHECK(cudaGetLastError());
     CATMSM_CHECK(cudaMemcpyAsync(w->h_out.p, w->out.p, (size_t)nmsm * sizeof(jac), cudaMemcpyDeviceToHost, st));

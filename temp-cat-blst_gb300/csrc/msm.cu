@@ -21,8 +21,10 @@
 //                    fixed chunk of L sorted entries and folds runs of equal
 //                    keys with XYZZ mixed adds; runs that cross a chunk edge
 //                    go to head/tail carry slots.
-//   5. k_fixup       joins carry slots of buckets that span chunks (block-wide
-//                    tree for buckets spanning many chunks: k_fixup_hot).
+//   5. k_fixup_seg / k_fixup_join  join the carry slots of buckets that span
+//                    chunks: a tree over each warp's chunks, then one piece
+//                    per warp (block-wide tree for very long spans:
+//                    k_fixup_hot_seg).
 //   6. k_reduce_level  sum_d d * S_d per window as a tree of running sums:
 //                    fan-in 8 over the buckets, then fan-in 2 levels whose
 //                    dependent chains are ~3 group operations (no scalar
@@ -444,6 +446,124 @@ __global__ void __launch_bounds__(kHotThreads) k_fixup_hot(const uint2* __restri
     }
 }
 
+// Segmented fixup (the MSM and batch pipelines; the fixed-scratch entry keeps
+// the serial k_fixup above).  A bucket spanning chunks t0..t1 is the sum of
+// tail[t0] and head[t0+1..t1].  k_fixup_seg reduces the head partials of
+// each warp's chunks per bucket with a tree over lanes (depth 5, one
+// addition per partial) and writes each warp-local piece's sum to the
+// piece's first head slot; k_fixup_join then adds tail[t0] and one piece per
+// warp the bucket spans.  A 16-chunk bucket costs 4 + 1 dependent additions
+// instead of 15.
+constexpr uint32_t kNoKey = 0xffffffffu;
+constexpr uint32_t kHotSpanSeg = 128;
+
+__device__ __forceinline__ void shfl_down_xyzz(xyzz& o, const xyzz& v, int d)
+{
+    const uint32_t* pv = reinterpret_cast<const uint32_t*>(&v);
+    uint32_t* po = reinterpret_cast<uint32_t*>(&o);
+#pragma unroll
+    for (int k = 0; k < 48; k++) po[k] = __shfl_down_sync(0xffffffffu, pv[k], d);
+}
+
+__global__ void __launch_bounds__(128) k_fixup_seg(const uint32_t* __restrict__ sorted_key,
+                                                   const uint32_t* __restrict__ total_ptr, uint32_t L,
+                                                   xyzz* __restrict__ head)
+{
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t E = *total_ptr;
+    const size_t start = (size_t)t * L;
+    uint32_t hk = kNoKey;                     // bucket of head[t], if chunk t starts inside one
+    if (start < E && start > 0) {
+        const uint32_t kf = sorted_key[start];
+        if (sorted_key[start - 1] == kf) hk = kf;
+    }
+    xyzz v;
+    if (hk != kNoKey) load_xyzz(v, head + t);
+    else xyzz_set_inf(v);
+    const uint32_t prev = __shfl_up_sync(0xffffffffu, hk, 1);
+    const uint32_t starts = __ballot_sync(0xffffffffu, lane == 0 || prev != hk);
+    const uint32_t first = 31 - __clz(starts & (0xffffffffu >> (31 - lane)));
+    const uint32_t off = lane - first;        // position within the lane segment
+    for (int d = 1; d < 32; d <<= 1) {
+        xyzz o;
+        shfl_down_xyzz(o, v, d);
+        const uint32_t ok = __shfl_down_sync(0xffffffffu, hk, d);
+        if (hk != kNoKey && (off & (2 * d - 1)) == 0 && lane + d < 32 && ok == hk) xyzz_add(v, o);
+    }
+    if (hk != kNoKey && off == 0) store_xyzz(head + t, v);
+}
+
+__global__ void __launch_bounds__(128) k_fixup_join(const uint32_t* __restrict__ sorted_key,
+                                                    const uint32_t* __restrict__ offsets,
+                                                    const uint32_t* __restrict__ total_ptr, uint32_t L,
+                                                    xyzz* __restrict__ buckets, const xyzz* __restrict__ head,
+                                                    const xyzz* __restrict__ tail, uint2* __restrict__ hot_list,
+                                                    uint32_t* __restrict__ hot_count)
+{
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t E = *total_ptr;
+    const size_t start = (size_t)t * L;
+    if (start >= E) return;
+    const uint32_t end = (uint32_t)min((size_t)E, start + L);
+    const uint32_t last = sorted_key[end - 1];
+    if (!(end < E && sorted_key[end] == last)) return;                 // bucket ends here
+    const bool single = sorted_key[start] == last;
+    const bool starts_before = start > 0 && sorted_key[start - 1] == sorted_key[start];
+    if (single && starts_before) return;                               // a middle chunk
+    const uint32_t t1 = (offsets[last + 1] - 1) / L;                   // last chunk of this bucket
+    if (t1 - t + 1 > kHotSpanSeg) {
+        const uint32_t h = atomicAdd(hot_count, 1u);
+        hot_list[h] = make_uint2(last, t);
+        return;
+    }
+    xyzz acc, part;
+    load_xyzz(acc, tail + t);
+    for (uint32_t u = t + 1; u <= t1; u = (u | 31u) + 1) {           // one piece per warp
+        load_xyzz(part, head + u);
+        xyzz_add(acc, part);
+    }
+    store_xyzz(buckets + last, acc);
+}
+
+// k_fixup_hot over the pieces k_fixup_seg left: tail[t0], head[t0 + 1] and
+// the head slot at each later warp boundary up to t1.
+__global__ void __launch_bounds__(kHotThreads) k_fixup_hot_seg(const uint2* __restrict__ hot_list,
+                                                               const uint32_t* __restrict__ hot_count,
+                                                               const uint32_t* __restrict__ offsets, uint32_t L,
+                                                               xyzz* __restrict__ buckets,
+                                                               const xyzz* __restrict__ head,
+                                                               const xyzz* __restrict__ tail)
+{
+    __shared__ xyzz sh[kHotThreads];
+    const uint32_t nh = *hot_count;
+    for (uint32_t h = blockIdx.x; h < nh; h += gridDim.x) {
+        const uint2 e = hot_list[h];
+        const uint32_t key = e.x, t0 = e.y;
+        const uint32_t t1 = (offsets[key + 1] - 1) / L;
+        const uint32_t np = 2 + (t1 >> 5) - ((t0 + 1) >> 5);          // tail + pieces
+        xyzz acc, part;
+        xyzz_set_inf(acc);
+        for (uint32_t i = threadIdx.x; i < np; i += kHotThreads) {
+            const uint32_t u = i == 1 ? t0 + 1 : (((t0 + 1) | 31u) + 1 + 32 * (i - 2));
+            load_xyzz(part, i == 0 ? tail + t0 : head + u);
+            xyzz_add(acc, part);
+        }
+        sh[threadIdx.x] = acc;
+        __syncthreads();
+        for (int k = kHotThreads / 2; k > 0; k >>= 1) {
+            if ((int)threadIdx.x < k) {
+                xyzz a = sh[threadIdx.x];
+                xyzz_add(a, sh[threadIdx.x + k]);
+                sh[threadIdx.x] = a;
+            }
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) store_xyzz(buckets + key, sh[0]);
+        __syncthreads();
+    }
+}
+
 // ----------------------------------------------------------------- 6/7. reduce
 // Window sum W = sum_{b<B} (b+1) S_b.  Write F0(x) = sum_i i x_i.  Grouping the
 // inputs of a level in runs of F (node u owns children uF .. uF+F-1):
@@ -699,9 +819,19 @@ cudaError_t msm_device(Ctx* ctx, const void* d_points, const uint8_t* d_scalars,
     k_accumulate<<<div_up(chunks, 128), 128, 0, st>>>((const affine*)d_points, sorted_pt, sorted_key, total, L,
                                                       buckets, head, tail);
     mark(5);
-    k_fixup<<<div_up(chunks, 128), 128, 0, st>>>(sorted_key, offsets, total, L, buckets, head, tail, hot_list,
-                                                 hot_count);
-    k_fixup_hot<<<2 * kSMs, kHotThreads, 0, st>>>(hot_list, hot_count, offsets, L, buckets, head, tail);
+    if (nD > 2 * (size_t)L * M) {
+        // buckets average more than two chunks: tree over each warp's chunks
+        k_fixup_seg<<<div_up(chunks, 128), 128, 0, st>>>(sorted_key, total, L, head);
+        k_fixup_join<<<div_up(chunks, 128), 128, 0, st>>>(sorted_key, offsets, total, L, buckets, head, tail,
+                                                          hot_list, hot_count);
+        k_fixup_hot_seg<<<2 * kSMs, kHotThreads, 0, st>>>(hot_list, hot_count, offsets, L, buckets, head, tail);
+        g_stats.launches++;
+    } else {
+        // short spans: one thread joins each bucket's few carries
+        k_fixup<<<div_up(chunks, 128), 128, 0, st>>>(sorted_key, offsets, total, L, buckets, head, tail, hot_list,
+                                                     hot_count);
+        k_fixup_hot<<<2 * kSMs, kHotThreads, 0, st>>>(hot_list, hot_count, offsets, L, buckets, head, tail);
+    }
     mark(6);
     {
         // level 1: fan-in 8 over the buckets; then fan-in 2 to the root
