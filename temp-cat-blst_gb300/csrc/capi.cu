@@ -64,6 +64,28 @@ static unsigned log2_exact(size_t n)
 
 static void write_inf(blst_p1* ret) { std::memset(ret, 0, sizeof(*ret)); }
 
+// H2D of n points on the context's copy stream (created on first use),
+// ordered after the work already queued on the pipeline stream; *ready is
+// recorded after the copy.
+cudaError_t copy_points_async(Ctx* ctx, void* dst, const void* src, size_t bytes, cudaEvent_t* ready)
+{
+    if (!ctx->copy_stream) {
+        CATMSM_CHECK(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+        CATMSM_CHECK(cudaEventCreateWithFlags(&ctx->points_ready, cudaEventDisableTiming));
+    }
+    // the copy overwrites the points buffer: wait for earlier users of it
+    CATMSM_CHECK(cudaEventRecord(ctx->points_ready, ctx->stream));
+    CATMSM_CHECK(cudaStreamWaitEvent(ctx->copy_stream, ctx->points_ready, 0));
+    CATMSM_CHECK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, ctx->copy_stream));
+    const cudaError_t err = cudaEventRecord(ctx->points_ready, ctx->copy_stream);
+    if (err != cudaSuccess) {
+        cudaStreamSynchronize(ctx->copy_stream);   // nothing may read the caller's buffer after return
+        return err;
+    }
+    *ready = ctx->points_ready;
+    return cudaSuccess;
+}
+
 static void msm_entry(blst_p1* ret, const blst_p1_affine* const points[], size_t npoints,
                       const blst_byte* const scalars[], size_t nbits, blst_limb_t* scratch, bool explicit_window,
                       size_t window)
@@ -88,11 +110,15 @@ static void msm_entry(blst_p1* ret, const blst_p1_affine* const points[], size_t
     void* ds = ctx->msm.scalars.get(npoints * nbytes + 16);
     if (!dp || !ds) { write_inf(ret); return; }
     uint64_t out[18];
-    cudaError_t err = cudaMemcpyAsync(dp, hp, npoints * sizeof(blst_p1_affine), cudaMemcpyHostToDevice, ctx->stream);
+    // Scalars first on the pipeline stream; the points on the copy stream,
+    // overlapping the digit, scan and scatter stages (which need only the
+    // scalars).  The pipeline waits for points_ready before reading points.
+    cudaError_t err = cudaMemcpyAsync(ds, hs, npoints * nbytes, cudaMemcpyHostToDevice, ctx->stream);
+    cudaEvent_t ready = nullptr;
+    if (err == cudaSuccess) err = copy_points_async(ctx, dp, hp, npoints * sizeof(blst_p1_affine), &ready);
     if (err == cudaSuccess)
-        err = cudaMemcpyAsync(ds, hs, npoints * nbytes, cudaMemcpyHostToDevice, ctx->stream);
-    if (err == cudaSuccess)
-        err = msm_device(ctx, dp, (const uint8_t*)ds, (uint32_t)nbytes, npoints, (uint32_t)nbits, 0, out);
+        err = msm_device(ctx, dp, (const uint8_t*)ds, (uint32_t)nbytes, npoints, (uint32_t)nbits, 0, out, ready);
+    if (ready) cudaStreamSynchronize(ctx->copy_stream);   // the caller's points are not read after return
     if (err != cudaSuccess) { write_inf(ret); return; }
     std::memcpy(ret, out, sizeof(*ret));
 }

@@ -34,8 +34,13 @@ cudaError_t msm_setup_device();
 uint32_t msm_reduce_tail_max();
 void msm_reduce_tail(const void* inA, const void* inQ, uint32_t m, uint32_t D, void* outQ, cudaStream_t st);
 
+// H2D of `bytes` from src to dst on the context's copy stream, after the work
+// already queued on its pipeline stream; *ready is an event recorded after
+// the copy (pass it to msm_device as points_ready).
+cudaError_t copy_points_async(Ctx* ctx, void* dst, const void* src, size_t bytes, cudaEvent_t* ready);
+
 cudaError_t msm_device(Ctx* ctx, const void* d_points, const uint8_t* d_scalars, uint32_t stride,
-                       size_t n, uint32_t nbits, uint32_t c, uint64_t* out);
+                       size_t n, uint32_t nbits, uint32_t c, uint64_t* out, cudaEvent_t points_ready = nullptr);
 
 cudaError_t points_from_scalars_device(Ctx* ctx, const uint8_t* d_k32, size_t n, void* d_out);
 

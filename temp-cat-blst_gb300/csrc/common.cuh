@@ -65,7 +65,7 @@ struct PinnedBuf {
 // Device workspaces of one MSM pipeline instance.
 struct MsmWork {
     DevBuf points, scalars, digits, ranks, counts, offsets, block_sums, sorted_pt, sorted_key,
-        buckets, head, tail, seg, wins, total, status, misc, glv_pts, glv_sc;
+        buckets, head, tail, seg, wins, total, status, misc, glv_pts, glv_sc, glv_sign;
 };
 
 struct FftWork {
@@ -73,7 +73,7 @@ struct FftWork {
 };
 
 // Per-stage CUDA-event timing of the MSM pipeline (off by default).
-constexpr int kMsmStages = 8;   // prep (memsets, GLV split), digits, scan, scatter, accumulate, fixup, reduce, host fold
+constexpr int kMsmStages = 8;   // prep (memsets, GLV scalar split), digits, scan, scatter (+ GLV points), accumulate, fixup, reduce, host fold
 struct StageProfile {
     bool enabled = false;
     cudaEvent_t ev[kMsmStages + 1] = {};
@@ -90,6 +90,8 @@ struct Ctx {
     PinnedBuf h_points, h_scalars, h_out, h_values, h_meta;
     StageProfile prof;
     bool glv = true;   // GLV split of scalars wider than 128 bits (catmsm_msm_glv)
+    cudaStream_t copy_stream = nullptr;    // host->device point copies that overlap the scalar stages
+    cudaEvent_t points_ready = nullptr;
 };
 
 // Per-thread context bound to the thread's current device.

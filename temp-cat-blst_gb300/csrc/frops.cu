@@ -297,15 +297,17 @@ static bool fr_msm_run(blst_p1* ret, const blst_p1_affine points[], const blst_f
     uint32_t* ds = (uint32_t*)ctx->msm.scalars.get(npoints * 32 + 16);
     if (!dp || !ds) return false;
     cudaStream_t st = ctx->stream;
-    cudaError_t err = cudaMemcpyAsync(dp, points, npoints * sizeof(blst_p1_affine), cudaMemcpyHostToDevice, st);
-    if (err == cudaSuccess) err = cudaMemcpyAsync(ds, scalars, npoints * 32, cudaMemcpyHostToDevice, st);
+    cudaError_t err = cudaMemcpyAsync(ds, scalars, npoints * 32, cudaMemcpyHostToDevice, st);
+    cudaEvent_t ready = nullptr;
+    if (err == cudaSuccess) err = copy_points_async(ctx, dp, points, npoints * sizeof(blst_p1_affine), &ready);
     if (err == cudaSuccess) {
         k_fr_to_canonical<<<div_up(npoints, 256), 256, 0, st>>>(ds, (uint32_t)npoints);
         g_stats.launches++;
         err = cudaGetLastError();
     }
     uint64_t out[18];
-    if (err == cudaSuccess) err = msm_device(ctx, dp, (const uint8_t*)ds, 32, npoints, 255, 0, out);
+    if (err == cudaSuccess) err = msm_device(ctx, dp, (const uint8_t*)ds, 32, npoints, 255, 0, out, ready);
+    if (ready) cudaStreamSynchronize(ctx->copy_stream);   // the caller's points are not read after return
     if (err != cudaSuccess) return false;
     std::memcpy(ret, out, sizeof(*ret));
     return true;

@@ -4,13 +4,16 @@
 // multi_scalar.cpp:806-923).  The result is the same group element
 // sum_i (k_i mod 2^nbits) * P_i; the device pipeline is:
 //
-//   0. k_glv_prep    (scalars wider than 128 bits) the GLV split: the points
+//   0. k_glv_scalars (scalars wider than 128 bits) the GLV split: the points
 //                    are prime-order subgroup elements (the reference's
 //                    contract, blst_scalar.h:539), where phi(x, y) =
 //                    (beta x, y) = lambda P, so k P = s1 m1 P + s2 m2 phi(P)
 //                    with m1, m2 < 2^127: an n-point 255-bit MSM becomes a
 //                    2n-point 127-bit MSM with the same bucket entries and
-//                    half the windows to reduce and fold.
+//                    half the windows to reduce and fold.  k_glv_points
+//                    writes the signed points +-P, +-phi(P) just before the
+//                    accumulation, so a host copy of the points can overlap
+//                    the scalar stages.
 //   1. k_digits      signed c-bit window digits (carry recoding, digit in
 //                    [-2^(c-1), 2^(c-1)]), one thread per scalar; each nonzero
 //                    digit takes a rank in its bucket with one atomicAdd.
@@ -150,10 +153,11 @@ __device__ __forceinline__ void dec4(uint32_t* a)
 //   k1 >= (lambda+1)/2:  k1 -> k1 - lambda,  k2 -> k2 + 1
 //   k2 >= (lambda+1)/2:  k2 -> k2 - lambda - 1,  k1 -> k1 - 1
 // (the second uses lambda^2 = -lambda - 1 mod r).  Writes the 16-byte
-// magnitudes m1 -> gsc[i], m2 -> gsc[n + i] and the signed points
-// s1 P -> gpts[i], s2 phi(P) -> gpts[n + i].
-__global__ void k_glv_prep(const affine* __restrict__ pts, const uint8_t* __restrict__ scalars, uint32_t stride,
-                           uint32_t n, uint32_t nbits, affine* __restrict__ gpts, uint4* __restrict__ gsc)
+// magnitudes m1 -> gsc[i], m2 -> gsc[n + i] and the signs s1 | s2 << 1 ->
+// sgn[i].  Needs only the scalars, so it runs while the points may still be
+// in flight from the host.
+__global__ void k_glv_scalars(const uint8_t* __restrict__ scalars, uint32_t stride, uint32_t n, uint32_t nbits,
+                              uint4* __restrict__ gsc, uint8_t* __restrict__ sgn)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -182,6 +186,16 @@ __global__ void k_glv_prep(const affine* __restrict__ pts, const uint8_t* __rest
     }
     gsc[i] = make_uint4(m1[0], m1[1], m1[2], m1[3]);
     gsc[n + i] = make_uint4(m2[0], m2[1], m2[2], m2[3]);
+    sgn[i] = (uint8_t)((s1 ? 1 : 0) | (s2 ? 2 : 0));
+}
+
+// The signed points of the split: s1 P -> gpts[i], s2 phi(P) -> gpts[n + i].
+__global__ void k_glv_points(const affine* __restrict__ pts, const uint8_t* __restrict__ sgn, uint32_t n,
+                             affine* __restrict__ gpts)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t sg = sgn[i];
     affine p;
     load_affine(p.x, p.y, pts + i);
     affine a = p, b = p;
@@ -191,8 +205,8 @@ __global__ void k_glv_prep(const affine* __restrict__ pts, const uint8_t* __rest
         for (int w = 0; w < 12; w++) beta.v[w] = FP_BETA[w];
         fp_mul(b.x, p.x, beta);
         fp_canon(b.x, b.x);
-        if (s1) fp_neg(a.y, p.y);
-        if (s2) fp_neg(b.y, p.y);
+        if (sg & 1) fp_neg(a.y, p.y);
+        if (sg & 2) fp_neg(b.y, p.y);
     }
     store_affine(gpts + i, a);
     store_affine(gpts + n + i, b);
@@ -740,7 +754,7 @@ void msm_plan(const Ctx* ctx, size_t n, uint32_t nbits, uint32_t* c, uint32_t* w
 // Runs the device pipeline over device-resident points/scalars on the context
 // stream and returns the folded, normalised result in `out` (144 bytes).
 cudaError_t msm_device(Ctx* ctx, const void* d_points, const uint8_t* d_scalars, uint32_t stride,
-                       size_t n, uint32_t nbits, uint32_t c, uint64_t* out)
+                       size_t n, uint32_t nbits, uint32_t c, uint64_t* out, cudaEvent_t points_ready)
 {
     cudaStream_t st = ctx->stream;
     MsmWork& W = ctx->msm;
@@ -753,12 +767,19 @@ cudaError_t msm_device(Ctx* ctx, const void* d_points, const uint8_t* d_scalars,
         if (P.enabled) cudaEventRecord(P.ev[i], st);
     };
     mark(0);
+    // The points are read only from the point stage on (after the scatter):
+    // points_ready, if given, is an event on another stream (a host copy in
+    // flight) that the pipeline waits for just before that stage.
+    const affine* src_points = (const affine*)d_points;
+    affine* gpts = nullptr;
+    uint8_t* sgn = nullptr;
+    const size_t n_in = n;
     if (use_glv(ctx, n, nbits)) {
-        affine* gpts = (affine*)W.glv_pts.get(2 * n * sizeof(affine));
+        gpts = (affine*)W.glv_pts.get(2 * n * sizeof(affine));
         uint4* gsc = (uint4*)W.glv_sc.get(2 * n * sizeof(uint4));
-        if (!gpts || !gsc) return cudaErrorMemoryAllocation;
-        k_glv_prep<<<div_up(n, 128), 128, 0, st>>>((const affine*)d_points, d_scalars, stride, (uint32_t)n, nbits,
-                                                   gpts, gsc);
+        sgn = (uint8_t*)W.glv_sign.get(n);
+        if (!gpts || !gsc || !sgn) return cudaErrorMemoryAllocation;
+        k_glv_scalars<<<div_up(n, 128), 128, 0, st>>>(d_scalars, stride, (uint32_t)n, nbits, gsc, sgn);
         g_stats.launches++;
         d_points = gpts;
         d_scalars = reinterpret_cast<const uint8_t*>(gsc);
@@ -815,6 +836,11 @@ cudaError_t msm_device(Ctx* ctx, const void* d_points, const uint8_t* d_scalars,
     mark(3);
     k_scatter<<<div_up(nD, 256), 256, 0, st>>>(digits, ranks, offsets, (uint32_t)n, (uint32_t)nD, sorted_pt,
                                               sorted_key);
+    if (points_ready) CATMSM_CHECK(cudaStreamWaitEvent(st, points_ready, 0));
+    if (gpts) {
+        k_glv_points<<<div_up(n_in, 128), 128, 0, st>>>(src_points, sgn, (uint32_t)n_in, gpts);
+        g_stats.launches++;
+    }
     mark(4);
     k_accumulate<<<div_up(chunks, 128), 128, 0, st>>>((const affine*)d_points, sorted_pt, sorted_key, total, L,
                                                       buckets, head, tail);
