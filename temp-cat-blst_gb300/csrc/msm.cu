@@ -116,38 +116,6 @@ __device__ __forceinline__ void load_scalar(uint32_t* k, const uint8_t* s, uint3
 }
 
 // ----------------------------------------------------------------- 0. GLV split
-// (lambda + 1) / 2 and lambda + 1, little-endian words (lambda = z^2 - 1,
-// lambda^2 + lambda + 1 = r)
-__device__ __constant__ static const uint32_t GLV_HALF[4] = {0x80000000u, 0x00000000u, 0x8000d201u, 0x5622d200u};
-__device__ __constant__ static const uint32_t GLV_LAMBDA1[4] = {0x00000000u, 0x00000001u, 0x0001a402u, 0xac45a401u};
-
-__device__ __forceinline__ bool ge4(const uint32_t* a, const uint32_t* b)
-{
-    for (int i = 3; i >= 0; i--)
-        if (a[i] != b[i]) return a[i] > b[i];
-    return true;
-}
-
-__device__ __forceinline__ void sub4(uint32_t* o, const uint32_t* a, const uint32_t* b)
-{
-    uint64_t br = 0;
-    for (int i = 0; i < 4; i++) {
-        const uint64_t d = (uint64_t)a[i] - b[i] - br;
-        o[i] = (uint32_t)d;
-        br = (d >> 63) & 1;
-    }
-}
-
-__device__ __forceinline__ void inc4(uint32_t* a)
-{
-    for (int i = 0; i < 4 && ++a[i] == 0; i++) {}
-}
-
-__device__ __forceinline__ void dec4(uint32_t* a)
-{
-    for (int i = 0; i < 4 && a[i]-- == 0; i++) {}
-}
-
 // Thread i: k = k_i mod r = k1 + k2 lambda (0 <= k1 < lambda, k2 <= lambda + 1),
 // balanced to k = s1 m1 + s2 m2 lambda with m1, m2 <= (lambda + 1) / 2:
 //   k1 >= (lambda+1)/2:  k1 -> k1 - lambda,  k2 -> k2 + 1
@@ -163,27 +131,9 @@ __global__ void k_glv_scalars(const uint8_t* __restrict__ scalars, uint32_t stri
     if (i >= n) return;
     uint32_t k[8];
     load_scalar(k, scalars + (size_t)i * stride, stride, nbits);
-    while (fr_geq(k, FR_R)) fr_sub_r(k);
     uint32_t m1[4], m2[4];
-    fr_glv_split(m1, m2, k);
-    bool s1 = false, s2 = false;
-    if (ge4(m1, GLV_HALF)) {
-        sub4(m1, FR_LAMBDA, m1);
-        s1 = true;
-        inc4(m2);
-    }
-    if (ge4(m2, GLV_HALF)) {
-        sub4(m2, GLV_LAMBDA1, m2);
-        s2 = true;
-        if (s1) {
-            inc4(m1);
-        } else if ((m1[0] | m1[1] | m1[2] | m1[3]) == 0) {
-            m1[0] = 1;
-            s1 = true;
-        } else {
-            dec4(m1);
-        }
-    }
+    bool s1, s2;
+    fr_glv_balanced(m1, m2, s1, s2, k);
     gsc[i] = make_uint4(m1[0], m1[1], m1[2], m1[3]);
     gsc[n + i] = make_uint4(m2[0], m2[1], m2[2], m2[3]);
     sgn[i] = (uint8_t)((s1 ? 1 : 0) | (s2 ? 2 : 0));
