@@ -64,6 +64,17 @@ void blst_p1s_mult_pippenger_window(blst_p1 *ret, const blst_p1_affine *const po
                                     const blst_byte *const scalars[], size_t nbits, blst_limb_t *scratch,
                                     size_t window);
 
+/* Replaces blst_p1s_tile_pippenger (bindings/blst_scalar.h:605,
+ * blst/c_api.cpp:1585-1612 -> scalar/curve/multi_scalar.cpp:806-864): one
+ * signed window of the Pippenger MSM, ret = sum_i d_i P_i with d_i the Booth
+ * digit of bits [bit0, bit0 + window) of scalar i (overlap bit bit0 - 1;
+ * encode size min(nbits - bit0 + 1, window)).  npoints == 0, a NULL head or
+ * scratch, window outside [1, 24], nbits outside [1, 256] or bit0 >= nbits
+ * -> infinity.  The result is written normalised. */
+void blst_p1s_tile_pippenger(blst_p1 *ret, const blst_p1_affine *const points[], size_t npoints,
+                             const blst_byte *const scalars[], size_t nbits, blst_limb_t *scratch, size_t bit0,
+                             size_t window);
+
 /* Replaces blst_fr_fft_domain_len (bindings/blst_fft.h:52, blst/fft_c_api.cpp:128):
  * n + 2 for n a power of two in [1, 2^30], else 0. */
 size_t blst_fr_fft_domain_len(size_t n);

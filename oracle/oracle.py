@@ -75,6 +75,18 @@ class _Common:
         self._wpre = f("p1s_mult_wbits_precompute")
         self._wmsm = f("p1s_mult_wbits")
 
+    def tile(self, points: bytes, scalars: bytes, n: int, nbits: int, bit0: int, window: int) -> bytes:
+        """One signed window (p1s_tile_pippenger, contiguous descriptors) -> compressed."""
+        f = getattr(self.L, ("oracle_" if isinstance(self, Oracle) else "blst_") + "p1s_tile_pippenger")
+        f.argtypes = [_vp, _vp, _sz, _vp, _sz, _vp, _sz, _sz]
+        pbuf, sbuf = _buf(bytearray(points)), _buf(bytearray(scalars))
+        parr = (C.c_void_p * 2)(C.cast(pbuf, C.c_void_p), None)
+        sarr = (C.c_void_p * 2)(C.cast(sbuf, C.c_void_p), None)
+        scratch = (C.c_uint64 * ((192 << max(0, window - 1)) // 8 + 1))()
+        ret = bytearray(P1)
+        f(_buf(ret), parr, n, sarr, nbits, scratch, bit0, window)
+        return self.compress(bytes(ret))
+
     def wbits_table(self, points: bytes, n: int, wbits: int) -> bytes:
         """Contiguous-descriptor table precompute; returns the table bytes."""
         size = self.wbits_table_sizeof(wbits, n)

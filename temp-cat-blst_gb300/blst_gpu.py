@@ -137,6 +137,8 @@ def load(build_if_missing=True):
     L.blst_p1s_mult_batch_affine_fr_scratch_sizeof.argtypes = [_sz, _sz, _sz]
     L.blst_p1s_mult_batch_affine_fr.restype = C.c_bool
     L.blst_p1s_mult_batch_affine_fr.argtypes = [_vp, _vp, _vp, _sz, _vp, _sz, _sz, _sz]
+    L.blst_p1s_tile_pippenger.restype = None
+    L.blst_p1s_tile_pippenger.argtypes = [_vp, _vp, _sz, _vp, _sz, _vp, _sz, _sz]
     L.blst_p1s_mult_wbits_precompute_sizeof.restype = _sz
     L.blst_p1s_mult_wbits_precompute_sizeof.argtypes = [_sz, _sz]
     L.blst_p1s_mult_wbits_precompute.restype = None
@@ -225,6 +227,20 @@ def p1s_mult_wbits(table: bytes, wbits: int, n: int, scalars: bytes, nbits: int 
     scr = (C.c_uint64 * 4)() if scratch else None
     ret = bytearray(P1)
     L.blst_p1s_mult_wbits(_buf(ret), tb if table is not None else None, wbits, n, sarr, nbits, scr)
+    return bytes(ret)
+
+
+def p1s_tile_pippenger(points: bytes, scalars: bytes, npoints: int, nbits: int, bit0: int, window: int,
+                       scratch: bool = True) -> bytes:
+    """One signed window of the MSM (blst_p1s_tile_pippenger); 144-byte blst_p1."""
+    L = load()
+    pb = _buf(bytearray(points) if points else bytearray(96))
+    sb = _buf(bytearray(scalars) if scalars else bytearray(32))
+    parr = (C.c_void_p * 2)(_addr(pb), None)
+    sarr = (C.c_void_p * 2)(_addr(sb), None)
+    scr = (C.c_uint64 * 4)() if scratch else None
+    ret = bytearray(P1)
+    L.blst_p1s_tile_pippenger(_buf(ret), parr, npoints, sarr, nbits, scr, bit0, window)
     return bytes(ret)
 
 

@@ -217,6 +217,38 @@ void blst_p1s_mult_pippenger_window(blst_p1* ret, const blst_p1_affine* const po
     }
 }
 
+void blst_p1s_tile_pippenger(blst_p1* ret, const blst_p1_affine* const points[], size_t npoints,
+                             const blst_byte* const scalars[], size_t nbits, blst_limb_t* scratch, size_t bit0,
+                             size_t window)
+{
+    try {
+        if (!ret) return;
+        write_inf(ret);
+        if (npoints == 0 || !points || !scalars || !points[0] || !scalars[0] || !scratch || window < 1 ||
+            window > 24 || nbits == 0 || nbits > 256 || bit0 >= nbits || npoints > 0x7fffffffu)
+            return;
+        Ctx* ctx = get_ctx();
+        if (!ctx) return;
+        const size_t nbytes = (nbits + 7) / 8;
+        bool e1, e2;
+        const uint8_t* hp = gather(points, npoints, sizeof(blst_p1_affine), ctx->h_points, e1);
+        const uint8_t* hs = gather(scalars, npoints, nbytes, ctx->h_scalars, e2);
+        if (e1 || e2) return;
+        void* dp = ctx->msm.points.get(npoints * sizeof(blst_p1_affine));
+        void* ds = ctx->msm.scalars.get(npoints * nbytes + 16);
+        if (!dp || !ds) return;
+        uint64_t out[18];
+        cudaError_t err = cudaMemcpyAsync(dp, hp, npoints * sizeof(blst_p1_affine), cudaMemcpyHostToDevice, ctx->stream);
+        if (err == cudaSuccess) err = cudaMemcpyAsync(ds, hs, npoints * nbytes, cudaMemcpyHostToDevice, ctx->stream);
+        if (err == cudaSuccess)
+            err = msm_tile_device(ctx, dp, (const uint8_t*)ds, (uint32_t)nbytes, npoints, (uint32_t)nbits,
+                                  (uint32_t)bit0, (uint32_t)window, out);
+        if (err == cudaSuccess) std::memcpy(ret, out, sizeof(*ret));
+    } catch (...) {
+        if (ret) write_inf(ret);
+    }
+}
+
 size_t blst_fr_fft_domain_len(size_t n) { return valid_fft_size(n) ? n + 2 : 0; }
 
 bool blst_fr_fft_domain_init(blst_fr* domain, size_t domain_len, size_t n)

@@ -42,6 +42,12 @@ cudaError_t copy_points_async(Ctx* ctx, void* dst, const void* src, size_t bytes
 cudaError_t msm_device(Ctx* ctx, const void* d_points, const uint8_t* d_scalars, uint32_t stride,
                        size_t n, uint32_t nbits, uint32_t c, uint64_t* out, cudaEvent_t points_ready = nullptr);
 
+// One window of the reference's tile MSM (blst_p1s_tile_pippenger) over
+// device-resident inputs: sum_i d_i P_i with d_i the Booth digit of bits
+// [bit0, bit0 + window) of scalar i (window in [1, 24], bit0 < nbits).
+cudaError_t msm_tile_device(Ctx* ctx, const void* d_points, const uint8_t* d_scalars, uint32_t stride, size_t n,
+                            uint32_t nbits, uint32_t bit0, uint32_t window, uint64_t* out);
+
 cudaError_t points_from_scalars_device(Ctx* ctx, const uint8_t* d_k32, size_t n, void* d_out);
 
 cudaError_t fp_mul_test_device(Ctx* ctx, const uint64_t* d_a, const uint64_t* d_b, uint64_t* d_out, size_t n,

@@ -194,6 +194,40 @@ __global__ void k_digits(const uint8_t* __restrict__ scalars, uint32_t stride, u
     }
 }
 
+// One window of the reference's tile (blst_p1s_tile_pippenger, c_api.cpp:
+// 1585-1612 -> multi_scalar.cpp:806-864; WindowExtract, multi_scalar.h:
+// 350-404): bits [bit0, bit0 + window) of each scalar with the bit below as
+// the overlap (none at bit0 = 0), Booth-encoded over enc = min(nbits - bit0
+// + 1, window) bits: digit magnitude in [0, 2^(enc-1)], bucket |d| - 1.
+__global__ void k_tile_digits(const uint8_t* __restrict__ scalars, uint32_t stride, uint32_t n, uint32_t nbits,
+                              uint32_t bit0, uint32_t window, uint32_t enc, uint32_t* __restrict__ digits,
+                              uint32_t* __restrict__ ranks, uint32_t* __restrict__ counts)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t k[9];
+    load_scalar(k, scalars + (size_t)i * stride, stride, nbits);
+    k[8] = 0;
+    const uint32_t begin = bit0 > 0 ? bit0 - 1 : 0;
+    const uint32_t endb = min(bit0 + window, nbits);
+    const uint32_t size = endb - begin;                    // <= 25
+    const uint32_t word = begin >> 5, sh = begin & 31;
+    uint32_t v = k[word] >> sh;
+    if (sh && word + 1 < 9) v |= k[word + 1] << (32 - sh);
+    v &= (1u << size) - 1;
+    if (bit0 == 0) v <<= 1;                                 // no overlap bit below bit 0
+    const uint32_t sign = (v >> enc) & 1;
+    const uint32_t val = (v + 1) >> 1;
+    const uint32_t mag = sign ? (1u << enc) - val : val;
+    if (mag == 0) {
+        digits[i] = 0xffffffffu;
+        return;
+    }
+    const uint32_t key = mag - 1;
+    ranks[i] = atomicAdd(&counts[key], 1u);
+    digits[i] = key | (sign ? 0x80000000u : 0u);
+}
+
 // ----------------------------------------------------------------- 2. scan
 constexpr int kScanThreads = 1024;
 constexpr int kScanPer = 4;
@@ -703,8 +737,11 @@ void msm_plan(const Ctx* ctx, size_t n, uint32_t nbits, uint32_t* c, uint32_t* w
 
 // Runs the device pipeline over device-resident points/scalars on the context
 // stream and returns the folded, normalised result in `out` (144 bytes).
-cudaError_t msm_device(Ctx* ctx, const void* d_points, const uint8_t* d_scalars, uint32_t stride,
-                       size_t n, uint32_t nbits, uint32_t c, uint64_t* out, cudaEvent_t points_ready)
+// tile_window != 0: one window of the reference's tile (bit0, window) instead
+// of the whole MSM (no GLV split, D = 1, c = the window's encode size).
+static cudaError_t msm_run(Ctx* ctx, const void* d_points, const uint8_t* d_scalars, uint32_t stride, size_t n,
+                           uint32_t nbits, uint32_t c, uint64_t* out, cudaEvent_t points_ready, uint32_t tile_bit0,
+                           uint32_t tile_window)
 {
     cudaStream_t st = ctx->stream;
     MsmWork& W = ctx->msm;
@@ -724,7 +761,7 @@ cudaError_t msm_device(Ctx* ctx, const void* d_points, const uint8_t* d_scalars,
     affine* gpts = nullptr;
     uint8_t* sgn = nullptr;
     const size_t n_in = n;
-    if (use_glv(ctx, n, nbits)) {
+    if (!tile_window && use_glv(ctx, n, nbits)) {
         gpts = (affine*)W.glv_pts.get(2 * n * sizeof(affine));
         uint4* gsc = (uint4*)W.glv_sc.get(2 * n * sizeof(uint4));
         sgn = (uint8_t*)W.glv_sign.get(n);
@@ -738,9 +775,16 @@ cudaError_t msm_device(Ctx* ctx, const void* d_points, const uint8_t* d_scalars,
         nbits = 127;
         if (c == 0) c = msm_glv_window(n);
     }
-    if (c == 0) c = msm_default_window(n);
-    if (c < 2 || c > 22) return cudaErrorInvalidValue;
-    const uint32_t D = nbits / c + 1;
+    uint32_t D;
+    if (tile_window) {
+        c = min(nbits - tile_bit0 + 1, tile_window);    // encode size
+        D = 1;
+        if (c < 1 || c > 24) return cudaErrorInvalidValue;
+    } else {
+        if (c == 0) c = msm_default_window(n);
+        if (c < 2 || c > 22) return cudaErrorInvalidValue;
+        D = nbits / c + 1;
+    }
     const uint32_t B = 1u << (c - 1);
     const size_t M = (size_t)D * B;
     const size_t nD = (size_t)n * D;
@@ -778,7 +822,12 @@ cudaError_t msm_device(Ctx* ctx, const void* d_points, const uint8_t* d_scalars,
     CATMSM_CHECK(cudaMemsetAsync(buckets, 0, M * sizeof(xyzz), st));
     CATMSM_CHECK(cudaMemsetAsync(hot_count, 0, 4, st));
     mark(1);
-    k_digits<<<div_up(n, 256), 256, 0, st>>>(d_scalars, stride, (uint32_t)n, nbits, c, D, digits, ranks, counts);
+    if (tile_window)
+        k_tile_digits<<<div_up(n, 256), 256, 0, st>>>(d_scalars, stride, (uint32_t)n, nbits, tile_bit0, tile_window, c,
+                                                      digits, ranks, counts);
+    else
+        k_digits<<<div_up(n, 256), 256, 0, st>>>(d_scalars, stride, (uint32_t)n, nbits, c, D, digits, ranks,
+                                                counts);
     mark(2);
     k_scan_local<<<nblocks, kScanThreads, 0, st>>>(counts, offsets, bsums, (uint32_t)M);
     k_scan_top<<<1, kScanThreads, 0, st>>>(bsums, nblocks, total);
@@ -871,6 +920,19 @@ cudaError_t msm_device(Ctx* ctx, const void* d_points, const uint8_t* d_scalars,
         P.calls++;
     }
     return cudaSuccess;
+}
+
+cudaError_t msm_device(Ctx* ctx, const void* d_points, const uint8_t* d_scalars, uint32_t stride, size_t n,
+                       uint32_t nbits, uint32_t c, uint64_t* out, cudaEvent_t points_ready)
+{
+    return msm_run(ctx, d_points, d_scalars, stride, n, nbits, c, out, points_ready, 0, 0);
+}
+
+cudaError_t msm_tile_device(Ctx* ctx, const void* d_points, const uint8_t* d_scalars, uint32_t stride, size_t n,
+                            uint32_t nbits, uint32_t bit0, uint32_t window, uint64_t* out)
+{
+    if (window < 1 || window > 24 || nbits == 0 || nbits > 256 || bit0 >= nbits) return cudaErrorInvalidValue;
+    return msm_run(ctx, d_points, d_scalars, stride, n, nbits, 0, out, nullptr, bit0, window);
 }
 
 }  // namespace catmsm

@@ -18,7 +18,9 @@ reference's own C ABI built from its sources (oracle/_ref/libblst_ref.so):
   * msm_fr_variants: blst_p1s_mult_fr and blst_p1s_mult_batch_affine_fr ->
             compressed, and the reference's scratch-size queries for both
 
-`--section wbits|msm_fr_variants` regenerates only that section of an
+  * tile:   blst_p1s_tile_pippenger -> compressed, per (n, nbits, bit0, window)
+
+`--section wbits|msm_fr_variants|tile` regenerates only that section of an
 existing file.
 """
 import hashlib
@@ -112,6 +114,26 @@ def fr_variants_section(o, r):
     return out
 
 
+TILE_CASES = [
+    # (seed, n, kind, nbits, dup, bit0, window)
+    (101, 1, 0, 255, False, 0, 4), (102, 100, 0, 255, False, 0, 8), (103, 100, 0, 255, False, 250, 8),
+    (104, 100, 0, 255, False, 254, 8), (105, 1000, 0, 255, False, 100, 13), (106, 1000, 1, 64, False, 60, 10),
+    (107, 257, 0, 7, False, 3, 3), (108, 500, 2, 255, False, 17, 1), (109, 4096, 0, 255, False, 128, 16),
+    (110, 300, 0, 256, False, 255, 5), (111, 2000, 2, 255, True, 40, 18), (112, 50, 0, 17, False, 0, 17),
+]
+
+
+def tile_section(o, r):
+    out = []
+    for seed, n, kind, nbits, dup, bit0, window in TILE_CASES:
+        pts, sc = msm_inputs(o, seed, n, kind, nbits, dup)
+        res = r.tile(pts, sc, n, nbits, bit0, window)
+        out.append({"seed": seed, "n": n, "kind": kind, "nbits": nbits, "dup": dup, "bit0": bit0,
+                    "window": window, "compressed": res.hex()})
+        print("tile", seed, n, nbits, bit0, window, res.hex()[:16], flush=True)
+    return out
+
+
 def main():
     large = "--large" in sys.argv
     build(ref=True)
@@ -119,7 +141,7 @@ def main():
     if "--section" in sys.argv:
         name = sys.argv[sys.argv.index("--section") + 1]
         g = json.load(open(OUT))
-        g[name] = {"wbits": wbits_section, "msm_fr_variants": fr_variants_section}[name](o, r)
+        g[name] = {"wbits": wbits_section, "msm_fr_variants": fr_variants_section, "tile": tile_section}[name](o, r)
         json.dump(g, open(OUT, "w"), indent=1)
         print("wrote", OUT)
         return
@@ -201,6 +223,7 @@ def main():
         print("fr_fft", seed, n, flush=True)
     g["wbits"] = wbits_section(o, r)
     g["msm_fr_variants"] = fr_variants_section(o, r)
+    g["tile"] = tile_section(o, r)
     if not large and os.path.exists(OUT):
         # keep previously generated large cases
         old = json.load(open(OUT))

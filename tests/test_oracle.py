@@ -255,3 +255,13 @@ def test_oracle_matches_fr_msm_variant_goldens(golden, oracle):
             pts = pts[:96 * k] + bytes(96) + pts[96 * (k + 1):]
         frs = _frs(oracle, c["seed"] + 1000, n)
         assert oracle.msm_fr(pts, frs, n).hex() == c["compressed"], (c["api"], n)
+
+
+def test_oracle_tile_matches_golden(golden, oracle):
+    """The oracle's restatement of blst_p1s_tile_pippenger against the
+    reference's outputs (edge windows: bit0 = 0, top windows, window 1)."""
+    cases = golden["tile"]
+    assert len(cases) >= 12
+    for c in cases:
+        pts, sc = _msm_inputs(oracle, c)
+        assert oracle.tile(pts, sc, c["n"], c["nbits"], c["bit0"], c["window"]).hex() == c["compressed"], c
