@@ -720,6 +720,40 @@ void msm_reduce_tail(const void* inA, const void* inQ, uint32_t m, uint32_t D, v
     k_reduce_tail<<<D, T, 2 * T * sizeof(xyzz), st>>>((const xyzz*)inA, (const xyzz*)inQ, m, (xyzz*)outQ);
 }
 
+// Entries per k_accumulate thread.  Small inputs: enough chunks to fill the
+// GPU (nD / (152 x 1024), at least 4).  Once a chunk of 48 fills every
+// resident block slot: the L in [48, 96] that minimises ceil(W / L) L, W =
+// entries per resident thread slot, i.e. the launch ends on (just under) a
+// whole number of waves instead of a short last wave (measured at 2^20, GLV:
+// L = 64 -> 3.4 waves, 7.35 ms; L = 72 -> 3.0 waves, 7.14 ms); ties go to the
+// larger L (fewer chunk carries to join).
+static uint32_t accumulate_chunk(size_t nD)
+{
+    static int slots_by_dev[64] = {0};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int slots = (dev >= 0 && dev < 64) ? slots_by_dev[dev] : 0;
+    if (slots == 0) {
+        int sms = 0, per_sm = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_accumulate, 128, 0);
+        slots = sms > 0 && per_sm > 0 ? sms * per_sm * 128 : kSMs * 4 * 128;
+        if (dev >= 0 && dev < 64) slots_by_dev[dev] = slots;
+    }
+    const double W = (double)nD / slots;
+    if (W < 48) {
+        size_t L = nD / ((size_t)kSMs * 1024);
+        return (uint32_t)(L < 4 ? 4 : (L > 64 ? 64 : L));
+    }
+    uint32_t best = 64;
+    double best_cost = 0;
+    for (uint32_t L = 48; L <= 96; L++) {
+        const double cost = std::ceil(W / L) * L;
+        if (L == 48 || cost <= best_cost) { best_cost = cost; best = L; }
+    }
+    return best;
+}
+
 static bool use_glv(const Ctx* ctx, size_t n, uint32_t nbits)
 {
     return ctx->glv && nbits > 128 && n < (1u << 30);
@@ -789,9 +823,7 @@ static cudaError_t msm_run(Ctx* ctx, const void* d_points, const uint8_t* d_scal
     const size_t M = (size_t)D * B;
     const size_t nD = (size_t)n * D;
     if (nD > 0xffffffffu - 1) return cudaErrorInvalidValue;
-    uint32_t L = (uint32_t)(nD / ((size_t)kSMs * 1024));
-    if (L < 4) L = 4;
-    if (L > 64) L = 64;
+    const uint32_t L = accumulate_chunk(nD);
     const size_t chunks = (nD + L - 1) / L;
     const uint32_t S = 8;                         // reduction fan-in per level
     const size_t lvl1 = (size_t)D * ((B + S - 1) / S);
