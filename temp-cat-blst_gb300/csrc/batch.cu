@@ -567,7 +567,7 @@ int catmsm_basis_autotune(void* handle, size_t nmsm, const size_t* counts, const
     float best = 1e30f;
     uint32_t bc = b->c, bl = b->L;
     const uint32_t cs[] = {9, 10, 11, 12, 13};
-    const uint32_t ls[] = {8, 16, 32};
+    const uint32_t ls[] = {8, 16, 32, 48, 64, 96, 128, 192, 256};   // chunk lengths (96 measured best at 1024 x ~1.4k)
     for (uint32_t cc : cs) {
         for (uint32_t ll : ls) {
             if (catmsm_basis_set_config(b, cc, ll) != 0) continue;
