@@ -361,6 +361,53 @@ def batched_fft_section(g, synth, torch, dev, steps, warmup, peak):
     return res
 
 
+def decode_section(g, synth, torch, dev, steps, warmup):
+    """Batched point decoding (the blst_p1_uncompress / blst_p1_deserialize /
+    blst_p1_affine_in_g1 semantics, one element per thread): 2^20 encodings
+    (4096 distinct seeded points repeated), host buffers, H2D/D2H inside the
+    timer.  Reported per configuration: decoded points per second."""
+    import ctypes as C
+    import numpy as np
+    n, m = 1 << 20, 4096
+    k = torch.frombuffer(bytearray(synth.point_scalars(17, m)), dtype=torch.uint8).to(dev)
+    d_pts = torch.empty(m * 96, dtype=torch.uint8, device=dev)
+    torch.cuda.synchronize()
+    assert g.load().catmsm_p1_affines_from_scalars_device(d_pts.data_ptr(), k.data_ptr(), m) == 0
+    aff = bytes(d_pts.cpu().numpy())
+    one = (1).to_bytes(48, "little")
+    canon = g.fp_mul(aff, one * (2 * m), 2 * m)               # x R * 1 / R: Montgomery -> canonical
+    comp, unc = bytearray(), bytearray()
+    for i in range(m):
+        x = int.from_bytes(canon[96 * i:96 * i + 48], "little")
+        y = int.from_bytes(canon[96 * i + 48:96 * i + 96], "little")
+        xb = bytearray(x.to_bytes(48, "big"))
+        unc += xb + y.to_bytes(48, "big")
+        xb[0] |= 0x80 | (0x20 if y > (P_MOD - 1) // 2 else 0)
+        comp += xb
+    comp = bytes(comp) * (n // m)
+    unc = bytes(unc) * (n // m)
+    L = g.load()
+    out = (C.c_char * (96 * n))()
+    errs = (C.c_int * n)()
+    res = {}
+    for name, fn, enc, grp in (("uncompress", L.catmsm_p1s_uncompress, comp, 0),
+                               ("uncompress_in_g1", L.catmsm_p1s_uncompress, comp, 1),
+                               ("deserialize", L.catmsm_p1s_deserialize, unc, 0),
+                               ("deserialize_in_g1", L.catmsm_p1s_deserialize, unc, 1)):
+        eb = C.c_char_p(enc)
+        for _ in range(max(1, warmup)):
+            assert fn(out, eb, n, errs, grp) == 0
+        ts = []
+        for _ in range(max(1, steps // 2)):
+            t = time.perf_counter()
+            assert fn(out, eb, n, errs, grp) == 0
+            ts.append(time.perf_counter() - t)
+        ok = all(e == 0 for e in list(errs)[:4096])
+        res[name] = {"points_per_s": n / statistics.mean(ts), "ms": statistics.mean(ts) * 1e3, "all_ok": ok}
+    res["workload"] = "2^20 encodings (4096 distinct seeded G1 points repeated), host buffers"
+    return res
+
+
 def serving_section(g, synth, torch, dev, rates, seconds):
     """BASELINE config 5: Poisson arrivals (swept rate) of 70% MSMs with k
     log-uniform in [2^10, 2^22] over a resident 2^22-point basis (fixed-base
@@ -506,8 +553,12 @@ def run_ours(args, ws, rank, local):
     if args.only:
         # one section alone (a diagnostic line, e.g. for an ncu launch list)
         peak = max(g.imad_peak_forms())
-        fn = {"batched": batched_section, "fft": batched_fft_section}[args.only]
-        print(json.dumps({"section": args.only, args.only: fn(g, synth, torch, dev, args.steps, args.warmup, peak)}))
+        if args.only == "decode":
+            out = decode_section(g, synth, torch, dev, args.steps, args.warmup)
+        else:
+            fn = {"batched": batched_section, "fft": batched_fft_section}[args.only]
+            out = fn(g, synth, torch, dev, args.steps, args.warmup, peak)
+        print(json.dumps({"section": args.only, args.only: out}))
         return 0
 
     # ---- seeded inputs, resident in HBM
@@ -692,8 +743,8 @@ def main():
     ap.add_argument("--window", type=int, default=0, help="MSM window width (0 = library default)")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched MSM / FFT sections")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving sweep")
-    ap.add_argument("--only", choices=["batched", "fft"], default=None,
-                    help="run only the batched-commitments or batched-FFT section (diagnostic line)")
+    ap.add_argument("--only", choices=["batched", "fft", "decode"], default=None,
+                    help="run only the batched-commitments, batched-FFT or decoding section (diagnostic line)")
     ap.add_argument("--serve-rates", default="25,50,100,150", help="Poisson arrival rates (requests/s)")
     ap.add_argument("--serve-seconds", type=float, default=3.0, help="arrival window per rate")
     args = ap.parse_args()
