@@ -194,6 +194,38 @@ def test_msm_linearity_full_size(gpu, oracle, synth):
     assert got == exp
 
 
+def test_msm_linearity_max_size(gpu, oracle, synth):
+    """n = 2^24 (the pipeline at 2^25 GLV points, ~12 GB of device working
+    set) through the device-resident entry: sum k_i P_i == (sum k_i s_i mod
+    r) G, the sums of products taken with numpy in 32-bit limbs."""
+    import numpy as np
+    import torch
+    n = 1 << 24
+    s = synth.point_scalars(4444, n)
+    k = synth.scalars(4545, n, 0)
+    ks = torch.frombuffer(bytearray(s), dtype=torch.uint8).cuda()
+    dp = torch.empty(n * 96, dtype=torch.uint8, device="cuda")
+    torch.cuda.synchronize()
+    assert gpu.load().catmsm_p1_affines_from_scalars_device(dp.data_ptr(), ks.data_ptr(), n) == 0
+    del ks
+    dk = torch.frombuffer(bytearray(k), dtype=torch.uint8).cuda()
+    torch.cuda.synchronize()
+    got = oracle.compress(gpu.msm_device(dp.data_ptr(), dk.data_ptr(), 32, n, 255, 0))
+    # sum_i s_i k_i from the 64 limb-pair columns: the low and high 32-bit
+    # halves of the 64-bit products are summed separately (each sum < 2^56)
+    sv = np.frombuffer(s, dtype=np.uint32).reshape(n, 8).astype(np.uint64)
+    kv = np.frombuffer(k, dtype=np.uint32).reshape(n, 8).astype(np.uint64)
+    total = 0
+    for i in range(8):
+        for j in range(8):
+            prod = sv[:, i] * kv[:, j]                         # < 2^64, exact
+            lo = int((prod & 0xffffffff).sum())
+            hi = int((prod >> 32).sum())
+            total += (lo + (hi << 32)) << (32 * (i + j))
+    exp = oracle.compress(oracle.mult(oracle.generator(), (total % R).to_bytes(32, "little"), 256))
+    assert got == exp
+
+
 def test_msm_hot_buckets(gpu, oracle, synth):
     """Every window puts all points in one bucket (equal scalars): the
     chunk-spanning fixup must stay parallel and exact."""
