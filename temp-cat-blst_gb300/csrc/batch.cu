@@ -338,10 +338,13 @@ static void enqueue_batch(const Basis* b, BatchWork* w, cudaStream_t st, uint32_
             inQ = bufQ[pp];
             break;
         }
-        const uint32_t F = first ? 8 : 2, lgF = first ? 3 : 1;
+        const uint32_t F = first ? 8 : 2;
         const uint32_t m_out = (m + F - 1) / F;
-        k_reduce_level<<<div_up((size_t)nmsm * m_out, 128), 128, 0, st>>>(inA, inQ, m, F, lgF, nmsm, first ? 1 : 0,
-                                                                          bufA[pp], bufQ[pp]);
+        if (first)
+            k_reduce_level<<<div_up((size_t)nmsm * m_out, 128), 128, 0, st>>>(inA, inQ, m, F, 3, nmsm, 1, bufA[pp],
+                                                                              bufQ[pp]);
+        else
+            msm_reduce_pair(inA, inQ, m, nmsm, bufA[pp], bufQ[pp], st);
         inA = bufA[pp];
         inQ = bufQ[pp];
         pp ^= 1;

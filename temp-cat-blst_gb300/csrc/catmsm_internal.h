@@ -33,6 +33,9 @@ cudaError_t msm_setup_device();
 // pairs (m <= msm_reduce_tail_max()); roots to outQ[0..D).
 uint32_t msm_reduce_tail_max();
 void msm_reduce_tail(const void* inA, const void* inQ, uint32_t m, uint32_t D, void* outQ, cudaStream_t st);
+// One binary reduction level (fan-in 2) over D sets of m (A, Q) pairs.
+void msm_reduce_pair(const void* inA, const void* inQ, uint32_t m, uint32_t D, void* outA, void* outQ,
+                     cudaStream_t st);
 
 // H2D of `bytes` from src to dst on the context's copy stream, after the work
 // already queued on its pipeline stream; *ready is an event recorded after

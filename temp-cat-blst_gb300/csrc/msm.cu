@@ -608,66 +608,93 @@ __global__ void __launch_bounds__(128) k_reduce_level(const xyzz* __restrict__ i
     store_xyzz(outQ + (size_t)w * m_out + u, tt);
 }
 
-// The last binary levels in one launch: block w reduces window w's m_in
-// (A, Q) pairs (m_in <= 2 blockDim.x, blockDim.x <= kTailThreads; the block
-// is sized to the first level's nodes so that many windows fit on an SM) to
-// its root Q in shared memory with
-// one barrier per level, instead of one launch and a global round trip per
-// level (each upper level is a ~2-operation dependent chain, so launch gaps
-// and memory latency dominated them).  A node's rule is k_reduce_level's
-// with fan-in 2: Q = A_1 + Q_0 + Q_1, A = 2 (A_0 + A_1); a node with one
-// child keeps Q_0 and doubles A_0.
-constexpr int kTailThreads = 256;
-constexpr size_t kTailShared = 2 * kTailThreads * sizeof(xyzz);
-
-__device__ __forceinline__ void tail_node(xyzz& A, xyzz& Q, const xyzz* a, const xyzz* q, uint32_t cnt, bool need_a)
+// Binary levels with two threads per node: the Q thread computes
+// Q = A_1 + Q_0 + Q_1 and the A thread A = 2 (A_0 + A_1), concurrently (one
+// thread doing both ran 3 additions and a doubling back to back; the level's
+// dependent chain is now 2 additions).  A node with one child keeps Q_0 and
+// doubles A_0.  This is k_reduce_level's rule with fan-in 2.
+__device__ __forceinline__ void pair_node(xyzz& out, const xyzz* a, const xyzz* q, uint32_t cnt, bool q_role)
 {
     xyzz b;
-    if (cnt == 2) {
-        load_xyzz(A, a + 1);
-        Q = A;
-        load_xyzz(b, q);
-        xyzz_add(Q, b);
-        load_xyzz(b, q + 1);
-        xyzz_add(Q, b);
-        if (need_a) {
-            load_xyzz(b, a);
-            xyzz_add(A, b);
+    if (q_role) {
+        load_xyzz(out, q);
+        if (cnt == 2) {
+            load_xyzz(b, a + 1);
+            xyzz_add(out, b);
+            load_xyzz(b, q + 1);
+            xyzz_add(out, b);
         }
     } else {
-        load_xyzz(Q, q);
-        if (need_a) load_xyzz(A, a);
+        load_xyzz(out, a);
+        if (cnt == 2) {
+            load_xyzz(b, a + 1);
+            xyzz_add(out, b);
+        }
+        xyzz_dbl(out);
     }
-    if (need_a) xyzz_dbl(A);
 }
+
+// One binary level over D windows of m_in (A, Q) pairs.  The role is uniform
+// per warp (even warps Q, odd warps A, each over 32 consecutive nodes): lanes
+// of one warp taking different roles would run both paths one after the other.
+__device__ __forceinline__ void pair_slot(uint32_t g, uint32_t& node, bool& q_role)
+{
+    node = (g >> 6) * 32 + (g & 31);
+    q_role = ((g >> 5) & 1) == 0;
+}
+
+__global__ void __launch_bounds__(128) k_reduce_pair(const xyzz* __restrict__ inA, const xyzz* __restrict__ inQ,
+                                                     uint32_t m_in, uint32_t D, xyzz* __restrict__ outA,
+                                                     xyzz* __restrict__ outQ)
+{
+    const uint32_t m_out = (m_in + 1) / 2;
+    uint32_t t;
+    bool q_role;
+    pair_slot(blockIdx.x * blockDim.x + threadIdx.x, t, q_role);
+    if (t >= D * m_out || (!q_role && m_out == 1)) return;
+    const uint32_t w = t / m_out, u = t % m_out;
+    const size_t base = (size_t)w * m_in + 2 * u;
+    xyzz r;
+    pair_node(r, inA + base, inQ + base, min(2u, m_in - 2 * u), q_role);
+    store_xyzz((q_role ? outQ : outA) + (size_t)w * m_out + u, r);
+}
+
+// The last binary levels in one launch: block w reduces window w's m_in
+// (A, Q) pairs (m_in <= kTailThreads, two threads per node placed as in
+// k_reduce_pair; the block is sized to the first level so that many windows
+// fit on an SM) to its root Q in shared memory with one barrier per level,
+// instead of one launch and a global round trip per level.
+constexpr int kTailThreads = 256;
+constexpr size_t kTailShared = kTailThreads * sizeof(xyzz);   // A and Q for kTailThreads / 2 nodes
 
 __global__ void __launch_bounds__(kTailThreads) k_reduce_tail(const xyzz* __restrict__ inA,
                                                               const xyzz* __restrict__ inQ, uint32_t m_in,
                                                               xyzz* __restrict__ outQ)
 {
     extern __shared__ __align__(16) unsigned char tail_smem[];
+    const uint32_t half = blockDim.x / 2;
     xyzz* shA = reinterpret_cast<xyzz*>(tail_smem);
-    xyzz* shQ = shA + blockDim.x;
-    const uint32_t w = blockIdx.x, t = threadIdx.x;
+    xyzz* shQ = shA + half;
+    const uint32_t w = blockIdx.x;
+    uint32_t t;
+    bool q_role;
+    pair_slot(threadIdx.x, t, q_role);
     uint32_t m = m_in;
     const xyzz* srcA = inA + (size_t)w * m_in;
     const xyzz* srcQ = inQ + (size_t)w * m_in;
     while (m > 1) {
         const uint32_t m_out = (m + 1) / 2;
-        xyzz A, Q;
-        const bool act = t < m_out;
-        if (act) tail_node(A, Q, srcA + 2 * t, srcQ + 2 * t, min(2u, m - 2 * t), m_out > 1);
+        xyzz r;
+        const bool act = t < m_out && (q_role || m_out > 1);
+        if (act) pair_node(r, srcA + 2 * t, srcQ + 2 * t, min(2u, m - 2 * t), q_role);
         __syncthreads();
-        if (act) {
-            shQ[t] = Q;
-            if (m_out > 1) shA[t] = A;
-        }
+        if (act) (q_role ? shQ : shA)[t] = r;
         __syncthreads();
         srcA = shA;
         srcQ = shQ;
         m = m_out;
     }
-    if (t == 0) store_xyzz(outQ + w, m_in == 1 ? srcQ[0] : shQ[0]);
+    if (threadIdx.x == 0) store_xyzz(outQ + w, m_in == 1 ? srcQ[0] : shQ[0]);
 }
 
 // ----------------------------------------------------------------- host driver
@@ -712,12 +739,20 @@ cudaError_t msm_setup_device()
     return cudaFuncSetAttribute(k_reduce_tail, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTailShared);
 }
 
-uint32_t msm_reduce_tail_max() { return 2 * kTailThreads; }
+uint32_t msm_reduce_tail_max() { return kTailThreads; }
 
 void msm_reduce_tail(const void* inA, const void* inQ, uint32_t m, uint32_t D, void* outQ, cudaStream_t st)
 {
-    const uint32_t T = ((m + 1) / 2 + 31) / 32 * 32;   // m <= 2 kTailThreads
-    k_reduce_tail<<<D, T, 2 * T * sizeof(xyzz), st>>>((const xyzz*)inA, (const xyzz*)inQ, m, (xyzz*)outQ);
+    const uint32_t T = ((m + 1) / 2 + 31) / 32 * 64;   // a Q warp and an A warp per 32 first-level nodes
+    k_reduce_tail<<<D, T, T * sizeof(xyzz), st>>>((const xyzz*)inA, (const xyzz*)inQ, m, (xyzz*)outQ);
+}
+
+void msm_reduce_pair(const void* inA, const void* inQ, uint32_t m, uint32_t D, void* outA, void* outQ,
+                     cudaStream_t st)
+{
+    const size_t threads = ((size_t)D * ((m + 1) / 2) + 31) / 32 * 64;
+    k_reduce_pair<<<div_up(threads, 128), 128, 0, st>>>((const xyzz*)inA, (const xyzz*)inQ, m, D, (xyzz*)outA,
+                                                        (xyzz*)outQ);
 }
 
 // Entries per k_accumulate thread.  Small inputs: enough chunks to fill the
@@ -899,17 +934,20 @@ static cudaError_t msm_run(Ctx* ctx, const void* d_points, const uint8_t* d_scal
         uint32_t m = B, pp = 0;
         bool first = true;
         while (m > 1) {
-            if (!first && m <= 2 * kTailThreads) {
+            if (!first && m <= kTailThreads) {
                 msm_reduce_tail(inA, inQ, m, D, bufQ[pp], st);
                 g_stats.launches++;
                 inQ = bufQ[pp];
                 m = 1;
                 break;
             }
-            const uint32_t F = first ? S : 2, lgF = first ? 3 : 1;
+            const uint32_t F = first ? S : 2;
             const uint32_t m_out = (m + F - 1) / F;
-            k_reduce_level<<<div_up((size_t)D * m_out, 128), 128, 0, st>>>(inA, inQ, m, F, lgF, D, first ? 1 : 0,
-                                                                          bufA[pp], bufQ[pp]);
+            if (first)
+                k_reduce_level<<<div_up((size_t)D * m_out, 128), 128, 0, st>>>(inA, inQ, m, F, 3, D, 1, bufA[pp],
+                                                                              bufQ[pp]);
+            else
+                msm_reduce_pair(inA, inQ, m, D, bufA[pp], bufQ[pp], st);
             g_stats.launches++;
             inA = bufA[pp];
             inQ = bufQ[pp];
