@@ -40,6 +40,7 @@
 #include "host_curve.hpp"
 #include "catmsm_internal.h"
 
+#include <algorithm>
 #include <cmath>
 #include <mutex>
 
@@ -372,11 +373,11 @@ __global__ void __launch_bounds__(128, 4) k_accumulate(const affine* __restrict_
 // ----------------------------------------------------------------- 5. fixup
 // A bucket whose entries cross chunk edges has partial sums in tail[t0]
 // (its first chunk) and head[t0+1 .. t1].  Short spans are joined by one
-// thread; spans longer than kHotSpan chunks (a bucket holding a large share
-// of all entries, e.g. a carry-only top window or repeated scalars) go to a
-// list that k_fixup_hot reduces with a whole block per bucket, so no serial
-// chain grows with n.
-constexpr uint32_t kHotSpan = 16;
+// thread; spans longer than kHotSpan chunks (the narrow top window's
+// buckets, repeated scalars) go to a list that k_fixup_hot reduces with one
+// warp per bucket and a tree as deep as the span, so no serial chain is
+// longer than kHotSpan additions.
+constexpr uint32_t kHotSpan = 4;
 constexpr int kHotThreads = 128;
 
 __global__ void __launch_bounds__(128) k_fixup(const uint32_t* __restrict__ sorted_key,
@@ -411,36 +412,50 @@ __global__ void __launch_bounds__(128) k_fixup(const uint32_t* __restrict__ sort
     store_xyzz(buckets + last, acc);
 }
 
+__device__ __forceinline__ void shfl_down_xyzz(xyzz& o, const xyzz& v, int d)
+{
+    const uint32_t* pv = reinterpret_cast<const uint32_t*>(&v);
+    uint32_t* po = reinterpret_cast<uint32_t*>(&o);
+#pragma unroll
+    for (int k = 0; k < 48; k++) po[k] = __shfl_down_sync(0xffffffffu, pv[k], d);
+}
+
+// Sum of `span` partials of one bucket by one warp: each lane adds every
+// 32nd partial, then a shuffle tree only as deep as the span needs (a span of
+// s <= 32 costs 1 + ceil(log2 s) dependent additions).
+template <class PartAt>
+__device__ __forceinline__ void warp_join(xyzz& acc, uint32_t span, uint32_t lane, PartAt part_at)
+{
+    xyzz part;
+    xyzz_set_inf(acc);
+    for (uint32_t i = lane; i < span; i += 32) {
+        load_xyzz(part, part_at(i));
+        xyzz_add(acc, part);
+    }
+    const uint32_t width = min(span, 32u);
+    for (uint32_t d = 1; d < width; d <<= 1) {
+        xyzz o;
+        shfl_down_xyzz(o, acc, (int)d);
+        if ((lane & (2 * d - 1)) == 0 && lane + d < width) xyzz_add(acc, o);
+    }
+}
+
 __global__ void __launch_bounds__(kHotThreads) k_fixup_hot(const uint2* __restrict__ hot_list,
                                                            const uint32_t* __restrict__ hot_count,
                                                            const uint32_t* __restrict__ offsets, uint32_t L,
                                                            xyzz* __restrict__ buckets, const xyzz* __restrict__ head,
                                                            const xyzz* __restrict__ tail)
 {
-    __shared__ xyzz sh[kHotThreads];
     const uint32_t nh = *hot_count;
-    for (uint32_t h = blockIdx.x; h < nh; h += gridDim.x) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t warps = gridDim.x * (blockDim.x / 32);
+    for (uint32_t h = (blockIdx.x * blockDim.x + threadIdx.x) / 32; h < nh; h += warps) {
         const uint2 e = hot_list[h];
         const uint32_t key = e.x, t0 = e.y;
         const uint32_t span = (offsets[key + 1] - 1) / L - t0 + 1;
-        xyzz acc, part;
-        xyzz_set_inf(acc);
-        for (uint32_t i = threadIdx.x; i < span; i += kHotThreads) {
-            load_xyzz(part, i == 0 ? tail + t0 : head + t0 + i);
-            xyzz_add(acc, part);
-        }
-        sh[threadIdx.x] = acc;
-        __syncthreads();
-        for (int k = kHotThreads / 2; k > 0; k >>= 1) {
-            if ((int)threadIdx.x < k) {
-                xyzz a = sh[threadIdx.x];
-                xyzz_add(a, sh[threadIdx.x + k]);
-                sh[threadIdx.x] = a;
-            }
-            __syncthreads();
-        }
-        if (threadIdx.x == 0) store_xyzz(buckets + key, sh[0]);
-        __syncthreads();
+        xyzz acc;
+        warp_join(acc, span, lane, [&](uint32_t i) { return i == 0 ? tail + t0 : head + t0 + i; });
+        if (lane == 0) store_xyzz(buckets + key, acc);
     }
 }
 
@@ -454,14 +469,6 @@ __global__ void __launch_bounds__(kHotThreads) k_fixup_hot(const uint2* __restri
 // instead of 15.
 constexpr uint32_t kNoKey = 0xffffffffu;
 constexpr uint32_t kHotSpanSeg = 128;
-
-__device__ __forceinline__ void shfl_down_xyzz(xyzz& o, const xyzz& v, int d)
-{
-    const uint32_t* pv = reinterpret_cast<const uint32_t*>(&v);
-    uint32_t* po = reinterpret_cast<uint32_t*>(&o);
-#pragma unroll
-    for (int k = 0; k < 48; k++) po[k] = __shfl_down_sync(0xffffffffu, pv[k], d);
-}
 
 __global__ void __launch_bounds__(128) k_fixup_seg(const uint32_t* __restrict__ sorted_key,
                                                    const uint32_t* __restrict__ total_ptr, uint32_t L,
@@ -533,32 +540,19 @@ __global__ void __launch_bounds__(kHotThreads) k_fixup_hot_seg(const uint2* __re
                                                                const xyzz* __restrict__ head,
                                                                const xyzz* __restrict__ tail)
 {
-    __shared__ xyzz sh[kHotThreads];
     const uint32_t nh = *hot_count;
-    for (uint32_t h = blockIdx.x; h < nh; h += gridDim.x) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t warps = gridDim.x * (blockDim.x / 32);
+    for (uint32_t h = (blockIdx.x * blockDim.x + threadIdx.x) / 32; h < nh; h += warps) {
         const uint2 e = hot_list[h];
         const uint32_t key = e.x, t0 = e.y;
         const uint32_t t1 = (offsets[key + 1] - 1) / L;
         const uint32_t np = 2 + (t1 >> 5) - ((t0 + 1) >> 5);          // tail + pieces
-        xyzz acc, part;
-        xyzz_set_inf(acc);
-        for (uint32_t i = threadIdx.x; i < np; i += kHotThreads) {
-            const uint32_t u = i == 1 ? t0 + 1 : (((t0 + 1) | 31u) + 1 + 32 * (i - 2));
-            load_xyzz(part, i == 0 ? tail + t0 : head + u);
-            xyzz_add(acc, part);
-        }
-        sh[threadIdx.x] = acc;
-        __syncthreads();
-        for (int k = kHotThreads / 2; k > 0; k >>= 1) {
-            if ((int)threadIdx.x < k) {
-                xyzz a = sh[threadIdx.x];
-                xyzz_add(a, sh[threadIdx.x + k]);
-                sh[threadIdx.x] = a;
-            }
-            __syncthreads();
-        }
-        if (threadIdx.x == 0) store_xyzz(buckets + key, sh[0]);
-        __syncthreads();
+        xyzz acc;
+        warp_join(acc, np, lane, [&](uint32_t i) {
+            return i == 0 ? tail + t0 : head + (i == 1 ? t0 + 1 : (((t0 + 1) | 31u) + 1 + 32 * (i - 2)));
+        });
+        if (lane == 0) store_xyzz(buckets + key, acc);
     }
 }
 
@@ -665,6 +659,7 @@ __global__ void __launch_bounds__(128) k_reduce_pair(const xyzz* __restrict__ in
 // fit on an SM) to its root Q in shared memory with one barrier per level,
 // instead of one launch and a global round trip per level.
 constexpr int kTailThreads = 256;
+constexpr size_t kFanIn8MinBuckets = size_t(1) << 18;   // all windows' buckets
 constexpr size_t kTailShared = kTailThreads * sizeof(xyzz);   // A and Q for kTailThreads / 2 nodes
 
 __global__ void __launch_bounds__(kTailThreads) k_reduce_tail(const xyzz* __restrict__ inA,
@@ -755,8 +750,8 @@ void msm_reduce_pair(const void* inA, const void* inQ, uint32_t m, uint32_t D, v
                                                         (xyzz*)outQ);
 }
 
-// Entries per k_accumulate thread.  Small inputs: enough chunks to fill the
-// GPU (nD / (152 x 1024), at least 4).  Once a chunk of 48 fills every
+// Entries per k_accumulate thread.  Small inputs: the L in [4, 48] of least
+// modelled accumulate + fixup time (below).  Once a chunk of 48 fills every
 // resident block slot: the L in [48, 96] that minimises ceil(W / L) L, W =
 // entries per resident thread slot, i.e. the launch ends on (just under) a
 // whole number of waves instead of a short last wave (measured at 2^20, GLV:
@@ -764,21 +759,45 @@ void msm_reduce_pair(const void* inA, const void* inQ, uint32_t m, uint32_t D, v
 // larger L (fewer chunk carries to join).
 static uint32_t accumulate_chunk(size_t nD)
 {
-    static int slots_by_dev[64] = {0};
+    static int slots_by_dev[64] = {0}, sms_by_dev[64] = {0};
     int dev = 0;
     cudaGetDevice(&dev);
-    int slots = (dev >= 0 && dev < 64) ? slots_by_dev[dev] : 0;
+    const bool cached = dev >= 0 && dev < 64;
+    int slots = cached ? slots_by_dev[dev] : 0, sms = cached ? sms_by_dev[dev] : 0;
     if (slots == 0) {
-        int sms = 0, per_sm = 0;
+        int per_sm = 0;
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_accumulate, 128, 0);
-        slots = sms > 0 && per_sm > 0 ? sms * per_sm * 128 : kSMs * 4 * 128;
-        if (dev >= 0 && dev < 64) slots_by_dev[dev] = slots;
+        if (sms <= 0 || per_sm <= 0) {
+            sms = kSMs;
+            per_sm = 4;
+        }
+        slots = sms * per_sm * 128;
+        if (cached) {
+            slots_by_dev[dev] = slots;
+            sms_by_dev[dev] = sms;
+        }
     }
     const double W = (double)nD / slots;
     if (W < 48) {
-        size_t L = nD / ((size_t)kSMs * 1024);
-        return (uint32_t)(L < 4 ? 4 : (L > 64 ? 64 : L));
+        // Less than about one full wave.  The accumulate time is the busiest
+        // SM's work, its blocks x L entries (below ~1.5 blocks per SM the
+        // chain of L dependent additions sets it instead), and the fixup
+        // costs about one addition per chunk:
+        //   cost(L) = max(blocks per SM, 1.5) L + 4.7e-4 nD / L
+        // in units of one entry of a resident block (fitted on GB300 to
+        // 2^10..2^17-point MSMs).
+        uint32_t best = 4;
+        double best_cost = 0;
+        for (uint32_t L = 4; L <= 48; L++) {
+            const double bpsm = std::ceil(std::ceil((double)nD / L / 128) / sms);
+            const double cost = std::max(bpsm, 1.5) * L + 4.7e-4 * (double)nD / L;
+            if (L == 4 || cost < best_cost) {
+                best_cost = cost;
+                best = L;
+            }
+        }
+        return best;
     }
     uint32_t best = 64;
     double best_cost = 0;
@@ -860,7 +879,11 @@ static cudaError_t msm_run(Ctx* ctx, const void* d_points, const uint8_t* d_scal
     if (nD > 0xffffffffu - 1) return cudaErrorInvalidValue;
     const uint32_t L = accumulate_chunk(nD);
     const size_t chunks = (nD + L - 1) / L;
-    const uint32_t S = 8;                         // reduction fan-in per level
+    // Level 1 of the reduction: fan-in 8 (about 2.4 additions per bucket, but
+    // a 19-operation dependent chain) when there are enough buckets to keep
+    // every SM busy; otherwise fan-in 2 with the pair kernel straight from the
+    // buckets (Q = B_0 + 2 B_1, A = 2 (B_0 + B_1): two operations per level).
+    const uint32_t S = M >= kFanIn8MinBuckets ? 8 : 2;
     const size_t lvl1 = (size_t)D * ((B + S - 1) / S);
     const size_t lvl2 = (size_t)D * ((B + 2 * S - 1) / (2 * S)) + D;
 
@@ -926,13 +949,14 @@ static cudaError_t msm_run(Ctx* ctx, const void* d_points, const uint8_t* d_scal
     }
     mark(6);
     {
-        // level 1: fan-in 8 over the buckets; then fan-in 2 to the root
+        // level 1: fan-in S over the buckets; then fan-in 2 to the root.  With
+        // fan-in 2 throughout, level 1 is the pair rule with Q = A = buckets.
         xyzz* bufA[2] = {seg, seg + 2 * lvl1};
         xyzz* bufQ[2] = {seg + lvl1, seg + 2 * lvl1 + lvl2};
         const xyzz* inA = buckets;
-        const xyzz* inQ = nullptr;
+        const xyzz* inQ = S == 2 ? buckets : nullptr;
         uint32_t m = B, pp = 0;
-        bool first = true;
+        bool first = S == 8;
         while (m > 1) {
             if (!first && m <= kTailThreads) {
                 msm_reduce_tail(inA, inQ, m, D, bufQ[pp], st);
