@@ -333,7 +333,7 @@ static void enqueue_batch(const Basis* b, BatchWork* w, cudaStream_t st, uint32_
     uint32_t m = B, pp = 0;
     bool first = true;
     while (m > 1) {
-        if (!first && m <= msm_reduce_tail_max()) {
+        if (!first && m <= msm_reduce_tail_max(nmsm)) {
             msm_reduce_tail(inA, inQ, m, nmsm, bufQ[pp], st);
             inQ = bufQ[pp];
             break;

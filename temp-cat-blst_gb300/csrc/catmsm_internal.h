@@ -30,8 +30,8 @@ void msm_plan(const Ctx* ctx, size_t n, uint32_t nbits, uint32_t* c, uint32_t* w
 cudaError_t msm_setup_device();
 
 // The fused last reduction levels for D independent sets of m (A, Q) XYZZ
-// pairs (m <= msm_reduce_tail_max()); roots to outQ[0..D).
-uint32_t msm_reduce_tail_max();
+// pairs (m <= msm_reduce_tail_max(D)); roots to outQ[0..D).
+uint32_t msm_reduce_tail_max(uint32_t D);
 void msm_reduce_tail(const void* inA, const void* inQ, uint32_t m, uint32_t D, void* outQ, cudaStream_t st);
 // One binary reduction level (fan-in 2) over D sets of m (A, Q) pairs.
 void msm_reduce_pair(const void* inA, const void* inQ, uint32_t m, uint32_t D, void* outA, void* outQ,

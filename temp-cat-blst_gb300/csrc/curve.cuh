@@ -321,4 +321,101 @@ static __device__ __noinline__ void jac_mult_glv(jac& out, const jac& P, const u
     out = acc;
 }
 
+// ---------------------------------------------------------------------------
+// Quad point operations: four consecutive lanes (a quad) hold the same
+// operands and perform one XYZZ addition or doubling together.  At each step
+// lane k of the quad computes one of the step's independent products (the
+// same fp_mul_call on lane-selected operands, so the lanes never diverge) and
+// the products are exchanged with width-4 shuffles under the quad's own mask.
+// An addition becomes 4 dependent multiplications instead of ~11.5, a
+// doubling 3 instead of ~8: for chains of few point operations in few
+// threads (the reduction's upper levels, carry joins) latency, not
+// multiplier throughput, is what costs.  Every lane ends with the result.
+// All control flow below depends only on the quad's shared operands, so the
+// four lanes stay converged; callers keep the quad's lanes together.
+struct quad_lane {
+    uint32_t k;      // position in the quad
+    uint32_t mask;   // the quad's four lanes
+};
+
+__device__ __forceinline__ quad_lane quad_of(uint32_t lane)
+{
+    return quad_lane{lane & 3u, 0xfu << (lane & 28u)};
+}
+
+__device__ __forceinline__ fp fp_bcast(const fp& v, int src, const quad_lane& q)
+{
+    fp r;
+#pragma unroll
+    for (int i = 0; i < 12; i++) r.v[i] = __shfl_sync(q.mask, v.v[i], src, 4);
+    return r;
+}
+
+__device__ __forceinline__ fp fp_pick(uint32_t k, const fp& a0, const fp& a1, const fp& a2, const fp& a3)
+{
+    fp r;
+#pragma unroll
+    for (int i = 0; i < 12; i++) r.v[i] = k == 0 ? a0.v[i] : k == 1 ? a1.v[i] : k == 2 ? a2.v[i] : a3.v[i];
+    return r;
+}
+
+// dbl-2008-s as xyzz_dbl: V = U^2, M = 3 X^2 | W = U V, S = X V, M^2, ZZ V |
+// M (S - X3), W Y, ZZZ W.
+__device__ __forceinline__ void xyzz_dbl_quad(xyzz& p, const quad_lane& q)
+{
+    if (xyzz_is_inf(p)) return;
+    fp U, r;
+    fp_dbl(U, p.y);
+    r = fp_mul_call(fp_pick(q.k, U, p.x, U, p.x), fp_pick(q.k, U, p.x, U, p.x));
+    const fp V = fp_bcast(r, 0, q);
+    fp M = fp_bcast(r, 1, q), t;
+    fp_dbl(t, M);
+    fp_add(M, t, M);
+    r = fp_mul_call(fp_pick(q.k, V, p.x, M, p.zz), fp_pick(q.k, U, V, M, V));
+    const fp W = fp_bcast(r, 0, q), S = fp_bcast(r, 1, q), MM = fp_bcast(r, 2, q);
+    p.zz = fp_bcast(r, 3, q);
+    fp_sub(t, MM, S);
+    fp_sub(p.x, t, S);
+    fp_sub(t, S, p.x);
+    r = fp_mul_call(fp_pick(q.k, M, W, p.zzz, p.zzz), fp_pick(q.k, t, p.y, W, W));
+    const fp a = fp_bcast(r, 0, q), b = fp_bcast(r, 1, q);
+    p.zzz = fp_bcast(r, 2, q);
+    fp_sub(p.y, a, b);
+}
+
+// p += q, add-2008-s as xyzz_add: U1, U2, S1, S2 | P^2, R^2, ZZ1 ZZ2,
+// ZZZ1 ZZZ2 | P PP, U1 PP, ZZ1 ZZ2 PP | R (Q - X3), S1 PPP, ZZZ1 ZZZ2 PPP.
+__device__ __forceinline__ void xyzz_add_quad(xyzz& p, const xyzz& o, const quad_lane& q)
+{
+    if (xyzz_is_inf(o)) return;
+    if (xyzz_is_inf(p)) {
+        p = o;
+        return;
+    }
+    fp r = fp_mul_call(fp_pick(q.k, p.x, o.x, p.y, o.y), fp_pick(q.k, o.zz, p.zz, o.zzz, p.zzz));
+    const fp U1 = fp_bcast(r, 0, q), S1 = fp_bcast(r, 2, q);
+    fp P = fp_bcast(r, 1, q), R = fp_bcast(r, 3, q);
+    fp_sub(P, P, U1);
+    fp_sub(R, R, S1);
+    if (fp_is_zero(P)) {
+        if (fp_is_zero(R)) xyzz_dbl_quad(p, q);
+        else xyzz_set_inf(p);
+        return;
+    }
+    r = fp_mul_call(fp_pick(q.k, P, R, p.zz, p.zzz), fp_pick(q.k, P, R, o.zz, o.zzz));
+    const fp PP = fp_bcast(r, 0, q), RR = fp_bcast(r, 1, q), T1 = fp_bcast(r, 2, q), T2 = fp_bcast(r, 3, q);
+    r = fp_mul_call(fp_pick(q.k, P, U1, T1, T1), PP);
+    const fp PPP = fp_bcast(r, 0, q), Qv = fp_bcast(r, 1, q);
+    p.zz = fp_bcast(r, 2, q);
+    fp t;
+    fp_sub(t, RR, PPP);
+    fp_sub(t, t, Qv);
+    fp_sub(p.x, t, Qv);
+    fp_sub(t, Qv, p.x);
+    r = fp_mul_call(fp_pick(q.k, R, S1, T2, T2), fp_pick(q.k, t, PPP, PPP, PPP));
+    const fp a = fp_bcast(r, 0, q), b = fp_bcast(r, 1, q);
+    p.zzz = fp_bcast(r, 2, q);
+    fp_sub(p.y, a, b);
+}
+
 }  // namespace catmsm

@@ -606,37 +606,52 @@ __global__ void __launch_bounds__(128) k_reduce_level(const xyzz* __restrict__ i
 // Q = A_1 + Q_0 + Q_1 and the A thread A = 2 (A_0 + A_1), concurrently (one
 // thread doing both ran 3 additions and a doubling back to back; the level's
 // dependent chain is now 2 additions).  A node with one child keeps Q_0 and
-// doubles A_0.  This is k_reduce_level's rule with fan-in 2.
-__device__ __forceinline__ void pair_node(xyzz& out, const xyzz* a, const xyzz* q, uint32_t cnt, bool q_role)
+// doubles A_0.  This is k_reduce_level's rule with fan-in 2.  Quad = true:
+// each of the two is a quad of lanes (quad point operations), for levels
+// too small to fill the GPU.
+template <bool Quad>
+__device__ __forceinline__ void add_op(xyzz& p, const xyzz& o, const quad_lane& q)
+{
+    if (Quad) xyzz_add_quad(p, o, q);
+    else xyzz_add(p, o);
+}
+
+template <bool Quad>
+__device__ __forceinline__ void pair_node(xyzz& out, const xyzz* a, const xyzz* q, uint32_t cnt, bool q_role,
+                                          const quad_lane& ql)
 {
     xyzz b;
     if (q_role) {
         load_xyzz(out, q);
         if (cnt == 2) {
             load_xyzz(b, a + 1);
-            xyzz_add(out, b);
+            add_op<Quad>(out, b, ql);
             load_xyzz(b, q + 1);
-            xyzz_add(out, b);
+            add_op<Quad>(out, b, ql);
         }
     } else {
         load_xyzz(out, a);
         if (cnt == 2) {
             load_xyzz(b, a + 1);
-            xyzz_add(out, b);
+            add_op<Quad>(out, b, ql);
         }
-        xyzz_dbl(out);
+        if (Quad) xyzz_dbl_quad(out, ql);
+        else xyzz_dbl(out);
     }
 }
 
-// One binary level over D windows of m_in (A, Q) pairs.  The role is uniform
-// per warp (even warps Q, odd warps A, each over 32 consecutive nodes): lanes
-// of one warp taking different roles would run both paths one after the other.
+// Thread g's node and role.  The role is uniform per warp (even warps Q, odd
+// warps A): lanes of one warp taking different roles would run both paths one
+// after the other.  A warp covers 32 nodes, or 8 with quads.
+template <bool Quad>
 __device__ __forceinline__ void pair_slot(uint32_t g, uint32_t& node, bool& q_role)
 {
-    node = (g >> 6) * 32 + (g & 31);
+    node = Quad ? (g >> 6) * 8 + ((g >> 2) & 7) : (g >> 6) * 32 + (g & 31);
     q_role = ((g >> 5) & 1) == 0;
 }
 
+// One binary level over D windows of m_in (A, Q) pairs.
+template <bool Quad>
 __global__ void __launch_bounds__(128) k_reduce_pair(const xyzz* __restrict__ inA, const xyzz* __restrict__ inQ,
                                                      uint32_t m_in, uint32_t D, xyzz* __restrict__ outA,
                                                      xyzz* __restrict__ outQ)
@@ -644,36 +659,41 @@ __global__ void __launch_bounds__(128) k_reduce_pair(const xyzz* __restrict__ in
     const uint32_t m_out = (m_in + 1) / 2;
     uint32_t t;
     bool q_role;
-    pair_slot(blockIdx.x * blockDim.x + threadIdx.x, t, q_role);
+    pair_slot<Quad>(blockIdx.x * blockDim.x + threadIdx.x, t, q_role);
     if (t >= D * m_out || (!q_role && m_out == 1)) return;
+    const quad_lane ql = quad_of(threadIdx.x & 31);
     const uint32_t w = t / m_out, u = t % m_out;
     const size_t base = (size_t)w * m_in + 2 * u;
     xyzz r;
-    pair_node(r, inA + base, inQ + base, min(2u, m_in - 2 * u), q_role);
-    store_xyzz((q_role ? outQ : outA) + (size_t)w * m_out + u, r);
+    pair_node<Quad>(r, inA + base, inQ + base, min(2u, m_in - 2 * u), q_role, ql);
+    if (!Quad || ql.k == 0) store_xyzz((q_role ? outQ : outA) + (size_t)w * m_out + u, r);
 }
 
 // The last binary levels in one launch: block w reduces window w's m_in
-// (A, Q) pairs (m_in <= kTailThreads, two threads per node placed as in
-// k_reduce_pair; the block is sized to the first level so that many windows
-// fit on an SM) to its root Q in shared memory with one barrier per level,
-// instead of one launch and a global round trip per level.
+// (A, Q) pairs to its root Q in shared memory with one barrier per level,
+// instead of one launch and a global round trip per level.  Threads are
+// placed as in k_reduce_pair, the block sized to the first level so that many
+// windows fit on an SM: m_in <= kTailThreads with one lane per role, m_in <=
+// kTailThreads / 4 with quads.
 constexpr int kTailThreads = 256;
-constexpr size_t kFanIn8MinBuckets = size_t(1) << 18;   // all windows' buckets
 constexpr size_t kTailShared = kTailThreads * sizeof(xyzz);   // A and Q for kTailThreads / 2 nodes
+constexpr size_t kFanIn8MinBuckets = size_t(1) << 18;   // all windows' buckets
+constexpr uint32_t kQuadMaxNodes = 8192;                  // a level of at most this many nodes uses quads
 
+template <bool Quad>
 __global__ void __launch_bounds__(kTailThreads) k_reduce_tail(const xyzz* __restrict__ inA,
                                                               const xyzz* __restrict__ inQ, uint32_t m_in,
                                                               xyzz* __restrict__ outQ)
 {
     extern __shared__ __align__(16) unsigned char tail_smem[];
-    const uint32_t half = blockDim.x / 2;
+    const uint32_t nodes = blockDim.x / (Quad ? 8 : 2);
     xyzz* shA = reinterpret_cast<xyzz*>(tail_smem);
-    xyzz* shQ = shA + half;
+    xyzz* shQ = shA + nodes;
     const uint32_t w = blockIdx.x;
+    const quad_lane ql = quad_of(threadIdx.x & 31);
     uint32_t t;
     bool q_role;
-    pair_slot(threadIdx.x, t, q_role);
+    pair_slot<Quad>(threadIdx.x, t, q_role);
     uint32_t m = m_in;
     const xyzz* srcA = inA + (size_t)w * m_in;
     const xyzz* srcQ = inQ + (size_t)w * m_in;
@@ -681,9 +701,9 @@ __global__ void __launch_bounds__(kTailThreads) k_reduce_tail(const xyzz* __rest
         const uint32_t m_out = (m + 1) / 2;
         xyzz r;
         const bool act = t < m_out && (q_role || m_out > 1);
-        if (act) pair_node(r, srcA + 2 * t, srcQ + 2 * t, min(2u, m - 2 * t), q_role);
+        if (act) pair_node<Quad>(r, srcA + 2 * t, srcQ + 2 * t, min(2u, m - 2 * t), q_role, ql);
         __syncthreads();
-        if (act) (q_role ? shQ : shA)[t] = r;
+        if (act && (!Quad || ql.k == 0)) (q_role ? shQ : shA)[t] = r;
         __syncthreads();
         srcA = shA;
         srcQ = shQ;
@@ -731,23 +751,45 @@ uint32_t msm_glv_window(size_t n2)
 
 cudaError_t msm_setup_device()
 {
-    return cudaFuncSetAttribute(k_reduce_tail, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTailShared);
+    CATMSM_CHECK(cudaFuncSetAttribute(k_reduce_tail<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)kTailShared));
+    return cudaFuncSetAttribute(k_reduce_tail<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTailShared);
 }
 
-uint32_t msm_reduce_tail_max() { return kTailThreads; }
+// The tail takes a window set once m <= msm_reduce_tail_max(): with quads
+// when there are few windows (the tail's levels are then latency-bound), one
+// lane per role otherwise.
+static bool tail_quads(uint32_t D) { return (size_t)D * (kTailThreads / 8) <= kQuadMaxNodes; }
+
+uint32_t msm_reduce_tail_max(uint32_t D) { return tail_quads(D) ? kTailThreads / 4 : kTailThreads; }
 
 void msm_reduce_tail(const void* inA, const void* inQ, uint32_t m, uint32_t D, void* outQ, cudaStream_t st)
 {
-    const uint32_t T = ((m + 1) / 2 + 31) / 32 * 64;   // a Q warp and an A warp per 32 first-level nodes
-    k_reduce_tail<<<D, T, T * sizeof(xyzz), st>>>((const xyzz*)inA, (const xyzz*)inQ, m, (xyzz*)outQ);
+    const uint32_t nodes = (m + 1) / 2;
+    if (tail_quads(D)) {
+        const uint32_t T = (nodes + 7) / 8 * 64;   // a Q warp and an A warp per 8 first-level nodes
+        k_reduce_tail<true><<<D, T, T / 8 * 2 * sizeof(xyzz), st>>>((const xyzz*)inA, (const xyzz*)inQ, m,
+                                                                     (xyzz*)outQ);
+    } else {
+        const uint32_t T = (nodes + 31) / 32 * 64;   // a Q warp and an A warp per 32 first-level nodes
+        k_reduce_tail<false><<<D, T, T / 2 * 2 * sizeof(xyzz), st>>>((const xyzz*)inA, (const xyzz*)inQ, m,
+                                                                      (xyzz*)outQ);
+    }
 }
 
 void msm_reduce_pair(const void* inA, const void* inQ, uint32_t m, uint32_t D, void* outA, void* outQ,
                      cudaStream_t st)
 {
-    const size_t threads = ((size_t)D * ((m + 1) / 2) + 31) / 32 * 64;
-    k_reduce_pair<<<div_up(threads, 128), 128, 0, st>>>((const xyzz*)inA, (const xyzz*)inQ, m, D, (xyzz*)outA,
-                                                        (xyzz*)outQ);
+    const size_t nodes = (size_t)D * ((m + 1) / 2);
+    if (nodes <= kQuadMaxNodes) {
+        const size_t threads = (nodes + 7) / 8 * 64;
+        k_reduce_pair<true><<<div_up(threads, 128), 128, 0, st>>>((const xyzz*)inA, (const xyzz*)inQ, m, D,
+                                                                  (xyzz*)outA, (xyzz*)outQ);
+    } else {
+        const size_t threads = (nodes + 31) / 32 * 64;
+        k_reduce_pair<false><<<div_up(threads, 128), 128, 0, st>>>((const xyzz*)inA, (const xyzz*)inQ, m, D,
+                                                                   (xyzz*)outA, (xyzz*)outQ);
+    }
 }
 
 // Entries per k_accumulate thread.  Small inputs: the L in [4, 48] of least
@@ -958,7 +1000,7 @@ static cudaError_t msm_run(Ctx* ctx, const void* d_points, const uint8_t* d_scal
         uint32_t m = B, pp = 0;
         bool first = S == 8;
         while (m > 1) {
-            if (!first && m <= kTailThreads) {
+            if (!first && m <= msm_reduce_tail_max(D)) {
                 msm_reduce_tail(inA, inQ, m, D, bufQ[pp], st);
                 g_stats.launches++;
                 inQ = bufQ[pp];
