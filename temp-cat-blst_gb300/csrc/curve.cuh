@@ -351,11 +351,14 @@ __device__ __forceinline__ fp fp_bcast(const fp& v, int src, const quad_lane& q)
     return r;
 }
 
+// Operand k of four, by masks: a chain of conditional selects on a per-lane
+// k measured ~1.7k cycles per pick on sm_103a against ~60 for this form.
 __device__ __forceinline__ fp fp_pick(uint32_t k, const fp& a0, const fp& a1, const fp& a2, const fp& a3)
 {
+    const uint32_t m0 = 0u - (k == 0), m1 = 0u - (k == 1), m2 = 0u - (k == 2), m3 = 0u - (k == 3);
     fp r;
 #pragma unroll
-    for (int i = 0; i < 12; i++) r.v[i] = k == 0 ? a0.v[i] : k == 1 ? a1.v[i] : k == 2 ? a2.v[i] : a3.v[i];
+    for (int i = 0; i < 12; i++) r.v[i] = (a0.v[i] & m0) | (a1.v[i] & m1) | (a2.v[i] & m2) | (a3.v[i] & m3);
     return r;
 }
 
