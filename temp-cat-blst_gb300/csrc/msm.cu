@@ -440,12 +440,40 @@ __device__ __forceinline__ void warp_join(xyzz& acc, uint32_t span, uint32_t lan
     }
 }
 
+// The same for a bucket too large for one warp (a narrow top window, one
+// repeated scalar): the whole block, span / blockDim additions per thread,
+// then a tree over lanes and over the block's warps.  Thread 0 gets the sum.
+constexpr uint32_t kWarpJoinMax = 128;   // larger spans are joined by a block
+
+template <class PartAt>
+__device__ __forceinline__ void block_join(xyzz& acc, uint32_t span, PartAt part_at, xyzz* sh)
+{
+    const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    xyzz part;
+    xyzz_set_inf(acc);
+    for (uint32_t i = threadIdx.x; i < span; i += blockDim.x) {
+        load_xyzz(part, part_at(i));
+        xyzz_add(acc, part);
+    }
+    for (uint32_t d = 1; d < 32; d <<= 1) {
+        xyzz o;
+        shfl_down_xyzz(o, acc, (int)d);
+        if ((lane & (2 * d - 1)) == 0) xyzz_add(acc, o);
+    }
+    __syncthreads();                       // sh is free (previous bucket done)
+    if (lane == 0) sh[wid] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0)
+        for (uint32_t w = 1; w < blockDim.x / 32; w++) xyzz_add(acc, sh[w]);
+}
+
 __global__ void __launch_bounds__(kHotThreads) k_fixup_hot(const uint2* __restrict__ hot_list,
                                                            const uint32_t* __restrict__ hot_count,
                                                            const uint32_t* __restrict__ offsets, uint32_t L,
                                                            xyzz* __restrict__ buckets, const xyzz* __restrict__ head,
                                                            const xyzz* __restrict__ tail)
 {
+    __shared__ xyzz sh[kHotThreads / 32];
     const uint32_t nh = *hot_count;
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t warps = gridDim.x * (blockDim.x / 32);
@@ -453,9 +481,19 @@ __global__ void __launch_bounds__(kHotThreads) k_fixup_hot(const uint2* __restri
         const uint2 e = hot_list[h];
         const uint32_t key = e.x, t0 = e.y;
         const uint32_t span = (offsets[key + 1] - 1) / L - t0 + 1;
+        if (span > kWarpJoinMax) continue;
         xyzz acc;
         warp_join(acc, span, lane, [&](uint32_t i) { return i == 0 ? tail + t0 : head + t0 + i; });
         if (lane == 0) store_xyzz(buckets + key, acc);
+    }
+    for (uint32_t h = blockIdx.x; h < nh; h += gridDim.x) {
+        const uint2 e = hot_list[h];
+        const uint32_t key = e.x, t0 = e.y;
+        const uint32_t span = (offsets[key + 1] - 1) / L - t0 + 1;
+        if (span <= kWarpJoinMax) continue;
+        xyzz acc;
+        block_join(acc, span, [&](uint32_t i) { return i == 0 ? tail + t0 : head + t0 + i; }, sh);
+        if (threadIdx.x == 0) store_xyzz(buckets + key, acc);
     }
 }
 
@@ -540,19 +578,32 @@ __global__ void __launch_bounds__(kHotThreads) k_fixup_hot_seg(const uint2* __re
                                                                const xyzz* __restrict__ head,
                                                                const xyzz* __restrict__ tail)
 {
+    __shared__ xyzz sh[kHotThreads / 32];
     const uint32_t nh = *hot_count;
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t warps = gridDim.x * (blockDim.x / 32);
+    auto piece = [&](uint32_t t0, uint32_t i) {
+        return i == 0 ? tail + t0 : head + (i == 1 ? t0 + 1 : (((t0 + 1) | 31u) + 1 + 32 * (i - 2)));
+    };
     for (uint32_t h = (blockIdx.x * blockDim.x + threadIdx.x) / 32; h < nh; h += warps) {
         const uint2 e = hot_list[h];
         const uint32_t key = e.x, t0 = e.y;
         const uint32_t t1 = (offsets[key + 1] - 1) / L;
         const uint32_t np = 2 + (t1 >> 5) - ((t0 + 1) >> 5);          // tail + pieces
+        if (np > kWarpJoinMax) continue;
         xyzz acc;
-        warp_join(acc, np, lane, [&](uint32_t i) {
-            return i == 0 ? tail + t0 : head + (i == 1 ? t0 + 1 : (((t0 + 1) | 31u) + 1 + 32 * (i - 2)));
-        });
+        warp_join(acc, np, lane, [&](uint32_t i) { return piece(t0, i); });
         if (lane == 0) store_xyzz(buckets + key, acc);
+    }
+    for (uint32_t h = blockIdx.x; h < nh; h += gridDim.x) {
+        const uint2 e = hot_list[h];
+        const uint32_t key = e.x, t0 = e.y;
+        const uint32_t t1 = (offsets[key + 1] - 1) / L;
+        const uint32_t np = 2 + (t1 >> 5) - ((t0 + 1) >> 5);
+        if (np <= kWarpJoinMax) continue;
+        xyzz acc;
+        block_join(acc, np, [&](uint32_t i) { return piece(t0, i); }, sh);
+        if (threadIdx.x == 0) store_xyzz(buckets + key, acc);
     }
 }
 
