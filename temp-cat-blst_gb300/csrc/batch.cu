@@ -287,7 +287,8 @@ static cudaError_t ensure_work(const Basis* b, BatchWork* w, uint32_t nmsm, size
 }
 
 // The device sequence of one batch (everything after the input copies).
-static void enqueue_batch(const Basis* b, BatchWork* w, cudaStream_t st, uint32_t nmsm, size_t cap)
+// Returns the number of kernels it launched.
+static uint32_t enqueue_batch(const Basis* b, BatchWork* w, cudaStream_t st, uint32_t nmsm, size_t cap)
 {
     const uint32_t c = b->c, D = b->D, L = b->L, B = 1u << (c - 1);
     const size_t M = (size_t)nmsm * B;
@@ -330,9 +331,10 @@ static void enqueue_batch(const Basis* b, BatchWork* w, cudaStream_t st, uint32_
     xyzz* bufQ[2] = {seg + lvl1, seg + 2 * lvl1 + lvl2};
     const xyzz* inA = buckets;
     const xyzz* inQ = nullptr;
-    uint32_t m = B, pp = 0;
+    uint32_t m = B, pp = 0, launches = 10;      // digits .. fixup_hot_seg (9) and batch_out
     bool first = true;
     while (m > 1) {
+        launches++;
         if (!first && m <= msm_reduce_tail_max(nmsm)) {
             msm_reduce_tail(inA, inQ, m, nmsm, bufQ[pp], st);
             inQ = bufQ[pp];
@@ -352,6 +354,7 @@ static void enqueue_batch(const Basis* b, BatchWork* w, cudaStream_t st, uint32_
         first = false;
     }
     k_batch_out<<<div_up(nmsm, 128), 128, 0, st>>>(inQ ? inQ : inA, nmsm, (jac*)w->out.p);
+    return launches;
 }
 
 // exact_cap: size the work for exactly the pairs of this batch (serving);
@@ -395,8 +398,7 @@ static cudaError_t run_batch(Basis* b, BatchWork* w, cudaStream_t st, blst_p1* o
         CATMSM_CHECK(cudaGraphLaunch(g.exec, st));
         g_stats.launches += 1;
     } else {
-        enqueue_batch(b, w, st, nmsm, cap);
-        g_stats.launches += 13;
+        g_stats.launches += enqueue_batch(b, w, st, nmsm, cap);
     }
     CATMSM_CHECK(cudaGetLastError());
     CATMSM_CHECK(cudaMemcpyAsync(w->h_out.p, w->out.p, (size_t)nmsm * sizeof(jac), cudaMemcpyDeviceToHost, st));

@@ -420,30 +420,34 @@ __device__ __forceinline__ void shfl_down_xyzz(xyzz& o, const xyzz& v, int d)
     for (int k = 0; k < 48; k++) po[k] = __shfl_down_sync(0xffffffffu, pv[k], d);
 }
 
-// Sum of `span` partials of one bucket by one warp: each lane adds every
-// 32nd partial, then a shuffle tree only as deep as the span needs (a span of
-// s <= 32 costs 1 + ceil(log2 s) dependent additions).
+// Sum of `span` partials of one bucket by one warp.
+// The warp's eight quads each add every 8th partial with quad point
+// operations, then a tree over the quads as deep as the span needs: a span
+// of s <= 8 costs 1 + ceil(log2 s) quad additions (~10k cycles each against
+// ~26k for one lane's addition).  Lane 0 ends with the sum.
 template <class PartAt>
 __device__ __forceinline__ void warp_join(xyzz& acc, uint32_t span, uint32_t lane, PartAt part_at)
 {
+    const quad_lane ql = quad_of(lane);
+    const uint32_t qi = lane >> 2;
     xyzz part;
     xyzz_set_inf(acc);
-    for (uint32_t i = lane; i < span; i += 32) {
+    for (uint32_t i = qi; i < span; i += 8) {
         load_xyzz(part, part_at(i));
-        xyzz_add(acc, part);
+        xyzz_add_quad(acc, part, ql);
     }
-    const uint32_t width = min(span, 32u);
+    const uint32_t width = min(span, 8u);
     for (uint32_t d = 1; d < width; d <<= 1) {
         xyzz o;
-        shfl_down_xyzz(o, acc, (int)d);
-        if ((lane & (2 * d - 1)) == 0 && lane + d < width) xyzz_add(acc, o);
+        shfl_down_xyzz(o, acc, (int)(4 * d));
+        if ((qi & (2 * d - 1)) == 0 && qi + d < width) xyzz_add_quad(acc, o, ql);
     }
 }
 
 // The same for a bucket too large for one warp (a narrow top window, one
 // repeated scalar): the whole block, span / blockDim additions per thread,
 // then a tree over lanes and over the block's warps.  Thread 0 gets the sum.
-constexpr uint32_t kWarpJoinMax = 128;   // larger spans are joined by a block
+constexpr uint32_t kWarpJoinMax = 160;   // larger spans are joined by a block
 
 template <class PartAt>
 __device__ __forceinline__ void block_join(xyzz& acc, uint32_t span, PartAt part_at, xyzz* sh)
@@ -807,12 +811,21 @@ cudaError_t msm_setup_device()
     return cudaFuncSetAttribute(k_reduce_tail<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTailShared);
 }
 
-// The tail takes a window set once m <= msm_reduce_tail_max(): with quads
+// The tail takes a window set once m <= msm_reduce_tail_max(D): with quads
 // when there are few windows (the tail's levels are then latency-bound), one
-// lane per role otherwise.
+// lane per role otherwise.  Above kTailMaxSets sets (a batch of MSMs) it is
+// not used: one block per set leaves the later levels of every block nearly
+// empty, and the global pair levels (many sets per launch) finish sooner
+// (1024 sets of 128 pairs: tail 0.81 ms; pair levels about a third of that).
+constexpr uint32_t kTailMaxSets = 64;
+
 static bool tail_quads(uint32_t D) { return (size_t)D * (kTailThreads / 8) <= kQuadMaxNodes; }
 
-uint32_t msm_reduce_tail_max(uint32_t D) { return tail_quads(D) ? kTailThreads / 4 : kTailThreads; }
+uint32_t msm_reduce_tail_max(uint32_t D)
+{
+    if (D > kTailMaxSets) return 1;
+    return tail_quads(D) ? kTailThreads / 4 : kTailThreads;
+}
 
 void msm_reduce_tail(const void* inA, const void* inQ, uint32_t m, uint32_t D, void* outQ, cudaStream_t st)
 {
