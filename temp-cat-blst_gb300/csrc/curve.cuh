@@ -421,4 +421,108 @@ __device__ __forceinline__ void xyzz_add_quad(xyzz& p, const xyzz& o, const quad
     fp_sub(p.y, a, b);
 }
 
+// dbl-2009-l as jac_dbl: X^2, Y^2, Y Z | B^2, (X + B)^2, E^2 | E (D - X3).
+__device__ __forceinline__ void jac_dbl_quad(jac& p, const quad_lane& q)
+{
+    if (jac_is_inf(p)) return;
+    fp r = fp_mul_call(fp_pick(q.k, p.x, p.y, p.y, p.y), fp_pick(q.k, p.x, p.y, p.z, p.z));
+    const fp A = fp_bcast(r, 0, q), B = fp_bcast(r, 1, q), YZ = fp_bcast(r, 2, q);
+    fp XB, E, t, D;
+    fp_add(XB, p.x, B);
+    fp_dbl(E, A);
+    fp_add(E, E, A);
+    r = fp_mul_call(fp_pick(q.k, B, XB, E, E), fp_pick(q.k, B, XB, E, E));
+    const fp C = fp_bcast(r, 0, q), T = fp_bcast(r, 1, q), F = fp_bcast(r, 2, q);
+    fp_sub(t, T, A);
+    fp_sub(t, t, C);
+    fp_dbl(D, t);
+    fp_sub(t, F, D);
+    fp_sub(p.x, t, D);
+    fp_sub(t, D, p.x);
+    fp_dbl(p.z, YZ);
+    r = fp_mul_call(E, t);                      // the same product on every lane
+    fp C8;
+    fp_dbl(C8, C);
+    fp_dbl(C8, C8);
+    fp_dbl(C8, C8);
+    fp_sub(p.y, r, C8);
+}
+
+// p += o as jac_add: Z1^2, Z2^2, Y1 Z2, Y2 Z1 | U1, U2, S1, S2 | H^2, R^2,
+// Z1 Z2 | U1 HH, H HH, Z1 Z2 H | R (V - X3), S1 HHH.
+__device__ __forceinline__ void jac_add_quad(jac& p, const jac& o, const quad_lane& q)
+{
+    if (jac_is_inf(o)) return;
+    if (jac_is_inf(p)) {
+        p = o;
+        return;
+    }
+    fp r = fp_mul_call(fp_pick(q.k, p.z, o.z, p.y, o.y), fp_pick(q.k, p.z, o.z, o.z, p.z));
+    const fp z1z1 = fp_bcast(r, 0, q), z2z2 = fp_bcast(r, 1, q), s1a = fp_bcast(r, 2, q), ra = fp_bcast(r, 3, q);
+    r = fp_mul_call(fp_pick(q.k, p.x, o.x, s1a, ra), fp_pick(q.k, z2z2, z1z1, z2z2, z1z1));
+    const fp u1 = fp_bcast(r, 0, q), s1 = fp_bcast(r, 2, q);
+    fp h = fp_bcast(r, 1, q), R = fp_bcast(r, 3, q);
+    fp_sub(h, h, u1);
+    fp_sub(R, R, s1);
+    if (fp_is_zero(h)) {
+        if (fp_is_zero(R)) jac_dbl_quad(p, q);
+        else jac_set_inf(p);
+        return;
+    }
+    r = fp_mul_call(fp_pick(q.k, h, R, p.z, p.z), fp_pick(q.k, h, R, o.z, o.z));
+    const fp HH = fp_bcast(r, 0, q), RR = fp_bcast(r, 1, q), Z12 = fp_bcast(r, 2, q);
+    r = fp_mul_call(fp_pick(q.k, u1, h, Z12, Z12), fp_pick(q.k, HH, HH, h, h));
+    const fp V = fp_bcast(r, 0, q), HHH = fp_bcast(r, 1, q);
+    p.z = fp_bcast(r, 2, q);
+    fp t;
+    fp_sub(t, RR, HHH);
+    fp_sub(t, t, V);
+    fp_sub(p.x, t, V);
+    fp_sub(t, V, p.x);
+    r = fp_mul_call(fp_pick(q.k, R, s1, s1, s1), fp_pick(q.k, t, HHH, HHH, HHH));
+    const fp a = fp_bcast(r, 0, q), b = fp_bcast(r, 1, q);
+    fp_sub(p.y, a, b);
+}
+
+// jac_mult_glv with quad operations: every lane of the quad passes the same
+// point and scalar and ends with the product.
+static __device__ __noinline__ void jac_mult_glv_quad(jac& out, const jac& P, const uint32_t* k1, const uint32_t* k2,
+                                                      const quad_lane q)
+{
+    int8_t d1[26], d2[26];
+    booth5_128(d1, k1);
+    booth5_128(d2, k2);
+    jac T[16];                                   // T[i] = (i + 1) P
+    T[0] = P;
+    T[1] = P;
+    jac_dbl_quad(T[1], q);
+#pragma unroll 1
+    for (int i = 2; i < 16; i++) {
+        if (i & 1) { T[i] = T[i / 2]; jac_dbl_quad(T[i], q); }
+        else { T[i] = T[i - 1]; jac_add_quad(T[i], P, q); }
+    }
+    fp beta;
+#pragma unroll
+    for (int i = 0; i < 12; i++) beta.v[i] = FP_BETA[i];
+    jac acc;
+    jac_set_inf(acc);
+    for (int i = 25; i >= 0; i--) {
+        if (i < 25)
+            for (int k = 0; k < 5; k++) jac_dbl_quad(acc, q);
+        const int a = d1[i], b = d2[i];
+        if (a) {
+            jac t = T[(a > 0 ? a : -a) - 1];
+            if (a < 0) jac_neg(t);
+            jac_add_quad(acc, t, q);
+        }
+        if (b) {
+            jac t = T[(b > 0 ? b : -b) - 1];
+            fp_mul(t.x, t.x, beta);
+            if (b < 0) jac_neg(t);
+            jac_add_quad(acc, t, q);
+        }
+    }
+    out = acc;
+}
+
 }  // namespace catmsm

@@ -111,14 +111,20 @@ __global__ void k_bitrev_multi(const jac* __restrict__ in, jac* __restrict__ out
 }
 
 // Stage `len` over every job with n >= len.  lst: for this stage, pairs of
-// (job id, exclusive prefix of n/2 butterflies), `cnt` entries.
+// (job id, exclusive prefix of n/2 butterflies), `cnt` entries.  Quad = true:
+// a quad of lanes per butterfly (quad point operations), for stages with too
+// few butterflies to fill the GPU, where the ~0.9M-cycle chain of one scalar
+// multiplication, not the multiplier throughput, sets the stage time.
+template <bool Quad>
 __global__ void __launch_bounds__(64) k_fft_stage_multi(jac* __restrict__ a, const FftJob* __restrict__ jobs,
                                                         const uint32_t* __restrict__ lst_job,
                                                         const uint32_t* __restrict__ lst_pre, uint32_t cnt,
                                                         uint32_t total, uint32_t len, const uint32_t* __restrict__ glv)
 {
-    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t gt = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t t = Quad ? gt >> 2 : gt;
     if (t >= total) return;
+    const quad_lane ql = quad_of(threadIdx.x & 31);
     const uint32_t e = find_range(lst_pre, cnt, t);
     const FftJob J = jobs[lst_job[e]];
     const uint32_t b = t - lst_pre[e];
@@ -142,30 +148,43 @@ __global__ void __launch_bounds__(64) k_fft_stage_multi(jac* __restrict__ a, con
         uint32_t idx = j * (J.n / len);
         if (J.inv_from_fwd) idx = J.n - idx;
         const uint32_t* r = glv + 8 * (size_t)(J.glv_off + idx);
-        jac_mult_glv(v, v, r, r + 4);
+        if (Quad) jac_mult_glv_quad(v, v, r, r + 4, ql);
+        else jac_mult_glv(v, v, r, r + 4);
     }
     jac s = u;
-    jac_add(s, v);
-    jac_neg(v);
-    jac_add(u, v);
-    store_jac(base + i0, s);
-    store_jac(base + i1, u);
+    if (Quad) {
+        jac_add_quad(s, v, ql);
+        jac_neg(v);
+        jac_add_quad(u, v, ql);
+        if (ql.k == 0) store_jac(base + i0, s);
+        if (ql.k == 1) store_jac(base + i1, u);
+    } else {
+        jac_add(s, v);
+        jac_neg(v);
+        jac_add(u, v);
+        store_jac(base + i0, s);
+        store_jac(base + i1, u);
+    }
 }
 
 // inverse scale (jobs with scaled != 0) and canonicalisation of every element
+template <bool Quad>
 __global__ void __launch_bounds__(64) k_fft_finish_multi(jac* __restrict__ a, const FftJob* __restrict__ jobs,
                                                          const uint32_t* __restrict__ pre, uint32_t njobs,
                                                          uint32_t total, const uint32_t* __restrict__ glv,
                                                          int do_scale)
 {
-    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t gt = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t t = Quad ? gt >> 2 : gt;
     if (t >= total) return;
+    const quad_lane ql = quad_of(threadIdx.x & 31);
     const FftJob J = jobs[find_range(pre, njobs, t)];
     jac v;
     load_jac(v, a + t);
     if (do_scale && J.scaled) {
         const uint32_t* r = glv + 8 * (size_t)(J.glv_off + J.n);
-        jac_mult_glv(v, v, r, r + 4);
+        if (Quad) jac_mult_glv_quad(v, v, r, r + 4, ql);
+        else jac_mult_glv(v, v, r, r + 4);
     }
     if (jac_is_inf(v)) {
         jac_set_inf(v);
@@ -174,7 +193,26 @@ __global__ void __launch_bounds__(64) k_fft_finish_multi(jac* __restrict__ a, co
         fp_canon(v.y, v.y);
         fp_canon(v.z, v.z);
     }
-    store_jac(a + t, v);
+    if (!Quad || ql.k == 0) store_jac(a + t, v);
+}
+
+// Launches with at most this many scalar multiplications use quads: four
+// lanes each still fit in one wave of resident threads, and the stage time is
+// one multiplication's latency, which quads cut ~1.8x.  Larger launches are
+// throughput-bound and keep one lane per butterfly (quads cost ~1.6x the
+// multiplier work).
+static size_t fft_quad_max()
+{
+    static size_t by_dev[64] = {0};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev >= 0 && dev < 64 && by_dev[dev]) return by_dev[dev];
+    int sms = 0, per_sm = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fft_stage_multi<true>, 64, 0);
+    size_t v = (sms > 0 && per_sm > 0) ? (size_t)sms * per_sm * 64 / 4 : (size_t)kSMs * 64;
+    if (dev >= 0 && dev < 64) by_dev[dev] = v;
+    return v;
 }
 
 // Runs every job of `specs` over the concatenated values in d_values
@@ -252,13 +290,22 @@ cudaError_t fft_run_multi(Ctx* ctx, void* d_values, const FftSpec* specs, size_t
     k_bitrev_multi<<<div_up(total, 256), 256, 0, st>>>((const jac*)d_values, tmp, d_jobs, d_vpre, (uint32_t)count,
                                                        (uint32_t)total);
     g_stats.launches++;
+    const size_t qmax = fft_quad_max();
     for (uint32_t s = 1; s <= maxlog; s++) {
-        k_fft_stage_multi<<<div_up(st_tot[s], 64), 64, 0, st>>>(tmp, d_jobs, d_lst_job + st_off[s], d_lst_pre + st_off[s],
-                                                                st_cnt[s], st_tot[s], 1u << s, glv);
+        if (st_tot[s] <= qmax)
+            k_fft_stage_multi<true><<<div_up(4 * (size_t)st_tot[s], 64), 64, 0, st>>>(
+                tmp, d_jobs, d_lst_job + st_off[s], d_lst_pre + st_off[s], st_cnt[s], st_tot[s], 1u << s, glv);
+        else
+            k_fft_stage_multi<false><<<div_up(st_tot[s], 64), 64, 0, st>>>(
+                tmp, d_jobs, d_lst_job + st_off[s], d_lst_pre + st_off[s], st_cnt[s], st_tot[s], 1u << s, glv);
         g_stats.launches++;
     }
-    k_fft_finish_multi<<<div_up(total, 64), 64, 0, st>>>(tmp, d_jobs, d_vpre, (uint32_t)count, (uint32_t)total, glv,
-                                                         any_scale ? 1 : 0);
+    if (any_scale && total <= qmax)
+        k_fft_finish_multi<true><<<div_up(4 * total, 64), 64, 0, st>>>(tmp, d_jobs, d_vpre, (uint32_t)count,
+                                                                       (uint32_t)total, glv, 1);
+    else
+        k_fft_finish_multi<false><<<div_up(total, 64), 64, 0, st>>>(tmp, d_jobs, d_vpre, (uint32_t)count,
+                                                                    (uint32_t)total, glv, any_scale ? 1 : 0);
     g_stats.launches++;
     CATMSM_CHECK(cudaGetLastError());
     CATMSM_CHECK(cudaMemcpyAsync(d_values, tmp, total * sizeof(jac), cudaMemcpyDeviceToDevice, st));
