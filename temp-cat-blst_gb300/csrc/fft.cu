@@ -16,14 +16,16 @@
 //                      level (a batch of transforms fills the GPU where one
 //                      small transform cannot); inside a job, threads map
 //                      first onto the non-trivial butterflies (j >= 1, one
-//                      GLV scalar multiplication in signed 4-bit windows
+//                      GLV scalar multiplication in signed 5-bit windows
 //                      each), then onto the
 //                      j == 0 butterflies, so a warp rarely mixes the two.
+//                      Launches small enough to fit one wave at four lanes
+//                      per butterfly use quad point operations.
 //   k_fft_finish_multi the inverse 1/n scale (one GLV multiplication per
 //                      element of scaled jobs) and canonical coordinates.
 // Each butterfly is ~1.7k Fp multiplications (~1M IMAD) against 576 bytes of
-// traffic, so the stages are IMAD-bound and read/write straight from HBM/L2;
-// staging tiles in shared memory would save nothing measurable.
+// traffic, so large stages are IMAD-bound and read/write straight from
+// HBM/L2; staging tiles in shared memory would save nothing measurable.
 #include "common.cuh"
 #include "curve.cuh"
 #include "fr.cuh"

@@ -24,14 +24,17 @@
 //                    fixed chunk of L sorted entries and folds runs of equal
 //                    keys with XYZZ mixed adds; runs that cross a chunk edge
 //                    go to head/tail carry slots.
-//   5. k_fixup_seg / k_fixup_join  join the carry slots of buckets that span
-//                    chunks: a tree over each warp's chunks, then one piece
-//                    per warp (block-wide tree for very long spans:
-//                    k_fixup_hot_seg).
-//   6. k_reduce_level  sum_d d * S_d per window as a tree of running sums:
-//                    fan-in 8 over the buckets, then fan-in 2 levels whose
-//                    dependent chains are ~3 group operations (no scalar
-//                    multiplications); one launch per level.
+//   5. k_fixup (+ k_fixup_hot), or k_fixup_seg / k_fixup_join (+
+//                    k_fixup_hot_seg) when buckets average more than two
+//                    chunks: join the carry slots of buckets that span
+//                    chunks; long spans go to a hot list joined by a warp
+//                    (quad point operations) or, above 160 partials, a block.
+//   6. k_reduce_level / k_reduce_pair / k_reduce_tail  sum_d d * S_d per
+//                    window as a tree of running sums (no scalar
+//                    multiplications): fan-in 8 (or the pair rule, for few
+//                    buckets) over the buckets, then fan-in 2 levels with the
+//                    Q and A of a node on two warps, quads on small levels,
+//                    and the last levels of every window in one launch.
 //   8. host          folds the D window sums: ret = 2^c ret + W_w, top first
 //                    (reference multi_scalar.cpp:913-922), then normalises.
 #include "common.cuh"
