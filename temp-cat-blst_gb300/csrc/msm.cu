@@ -728,30 +728,27 @@ __global__ void __launch_bounds__(128) k_reduce_pair(const xyzz* __restrict__ in
 }
 
 // The last binary levels in one launch: block w reduces window w's m_in
-// (A, Q) pairs to its root Q in shared memory with one barrier per level,
-// instead of one launch and a global round trip per level.  Threads are
-// placed as in k_reduce_pair, the block sized to the first level so that many
-// windows fit on an SM: m_in <= kTailThreads with one lane per role, m_in <=
-// kTailThreads / 4 with quads.
+// (A, Q) pairs (m_in <= kTailThreads / 4) to its root Q in shared memory with
+// one barrier per level, instead of one launch and a global round trip per
+// level.  Quads placed as in k_reduce_pair<true>; the block is sized to the
+// first level so that many windows fit on an SM.
 constexpr int kTailThreads = 256;
-constexpr size_t kTailShared = kTailThreads * sizeof(xyzz);   // A and Q for kTailThreads / 2 nodes
 constexpr size_t kFanIn8MinBuckets = size_t(1) << 18;   // all windows' buckets
 constexpr uint32_t kQuadMaxNodes = 8192;                  // a level of at most this many nodes uses quads
 
-template <bool Quad>
 __global__ void __launch_bounds__(kTailThreads) k_reduce_tail(const xyzz* __restrict__ inA,
                                                               const xyzz* __restrict__ inQ, uint32_t m_in,
                                                               xyzz* __restrict__ outQ)
 {
     extern __shared__ __align__(16) unsigned char tail_smem[];
-    const uint32_t nodes = blockDim.x / (Quad ? 8 : 2);
+    const uint32_t nodes = blockDim.x / 8;
     xyzz* shA = reinterpret_cast<xyzz*>(tail_smem);
     xyzz* shQ = shA + nodes;
     const uint32_t w = blockIdx.x;
     const quad_lane ql = quad_of(threadIdx.x & 31);
     uint32_t t;
     bool q_role;
-    pair_slot<Quad>(threadIdx.x, t, q_role);
+    pair_slot<true>(threadIdx.x, t, q_role);
     uint32_t m = m_in;
     const xyzz* srcA = inA + (size_t)w * m_in;
     const xyzz* srcQ = inQ + (size_t)w * m_in;
@@ -759,9 +756,9 @@ __global__ void __launch_bounds__(kTailThreads) k_reduce_tail(const xyzz* __rest
         const uint32_t m_out = (m + 1) / 2;
         xyzz r;
         const bool act = t < m_out && (q_role || m_out > 1);
-        if (act) pair_node<Quad>(r, srcA + 2 * t, srcQ + 2 * t, min(2u, m - 2 * t), q_role, ql);
+        if (act) pair_node<true>(r, srcA + 2 * t, srcQ + 2 * t, min(2u, m - 2 * t), q_role, ql);
         __syncthreads();
-        if (act && (!Quad || ql.k == 0)) (q_role ? shQ : shA)[t] = r;
+        if (act && ql.k == 0) (q_role ? shQ : shA)[t] = r;
         __syncthreads();
         srcA = shA;
         srcQ = shQ;
@@ -809,39 +806,24 @@ uint32_t msm_glv_window(size_t n2)
 
 cudaError_t msm_setup_device()
 {
-    CATMSM_CHECK(cudaFuncSetAttribute(k_reduce_tail<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)kTailShared));
-    return cudaFuncSetAttribute(k_reduce_tail<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTailShared);
+    return cudaFuncSetAttribute(k_reduce_tail, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)(kTailThreads / 8 * 2 * sizeof(xyzz)));
 }
 
-// The tail takes a window set once m <= msm_reduce_tail_max(D): with quads
-// when there are few windows (the tail's levels are then latency-bound), one
-// lane per role otherwise.  Above kTailMaxSets sets (a batch of MSMs) it is
-// not used: one block per set leaves the later levels of every block nearly
-// empty, and the global pair levels (many sets per launch) finish sooner
-// (1024 sets of 128 pairs: tail 0.81 ms; pair levels about a third of that).
+// The tail takes a window set once m <= msm_reduce_tail_max(D), with quads
+// (its levels are latency-bound).  Above kTailMaxSets sets (a batch of MSMs)
+// it is not used: one block per set leaves the later levels of every block
+// nearly empty, and the global pair levels (many sets per launch) finish
+// sooner (1024 sets of 128 pairs: tail 0.81 ms; pair levels about a third of
+// that).
 constexpr uint32_t kTailMaxSets = 64;
 
-static bool tail_quads(uint32_t D) { return (size_t)D * (kTailThreads / 8) <= kQuadMaxNodes; }
-
-uint32_t msm_reduce_tail_max(uint32_t D)
-{
-    if (D > kTailMaxSets) return 1;
-    return tail_quads(D) ? kTailThreads / 4 : kTailThreads;
-}
+uint32_t msm_reduce_tail_max(uint32_t D) { return D > kTailMaxSets ? 1 : kTailThreads / 4; }
 
 void msm_reduce_tail(const void* inA, const void* inQ, uint32_t m, uint32_t D, void* outQ, cudaStream_t st)
 {
-    const uint32_t nodes = (m + 1) / 2;
-    if (tail_quads(D)) {
-        const uint32_t T = (nodes + 7) / 8 * 64;   // a Q warp and an A warp per 8 first-level nodes
-        k_reduce_tail<true><<<D, T, T / 8 * 2 * sizeof(xyzz), st>>>((const xyzz*)inA, (const xyzz*)inQ, m,
-                                                                     (xyzz*)outQ);
-    } else {
-        const uint32_t T = (nodes + 31) / 32 * 64;   // a Q warp and an A warp per 32 first-level nodes
-        k_reduce_tail<false><<<D, T, T / 2 * 2 * sizeof(xyzz), st>>>((const xyzz*)inA, (const xyzz*)inQ, m,
-                                                                      (xyzz*)outQ);
-    }
+    const uint32_t T = ((m + 1) / 2 + 7) / 8 * 64;   // a Q warp and an A warp per 8 first-level nodes
+    k_reduce_tail<<<D, T, T / 8 * 2 * sizeof(xyzz), st>>>((const xyzz*)inA, (const xyzz*)inQ, m, (xyzz*)outQ);
 }
 
 void msm_reduce_pair(const void* inA, const void* inQ, uint32_t m, uint32_t D, void* outA, void* outQ,

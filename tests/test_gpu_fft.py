@@ -133,6 +133,47 @@ def test_fft_batch_matches_golden(gpu, oracle, golden):
         assert hashlib.sha256(ser).hexdigest() == c["sha256"], (n, c["mode"])
 
 
+def test_fft_batch_large_lane_per_butterfly(gpu, oracle, golden):
+    """The golden 4096-point cases, six copies each, in one batch: every stage
+    launch holds more butterflies than one wave fits at four lanes each, so
+    the stages and the inverse scale run one lane per butterfly (smaller
+    launches, as in the tests above, use quad point operations)."""
+    mode_of = {"dfwd": 0, "dinv": 1, "dunscaled": 2}
+    big = [c for c in golden["fft"] if c["mode"] in mode_of and c["n"] == 4096]
+    assert big
+    vals, ns, doms, modes, cases = [], [], [], [], []
+    d = gpu.fr_fft_domain_init(4096)[1]
+    for c in big:
+        v = oracle.jacobian_randomize(c["seed"], 4096, oracle.gen_points(c["seed"], 4096))
+        for _ in range(6):
+            vals.append(v)
+            ns.append(4096)
+            doms.append(d)
+            modes.append(mode_of[c["mode"]])
+            cases.append(c)
+    assert len(cases) * 2048 > 9728          # butterflies per stage launch; quads fit at most 9728 on a GB300
+    rc, outs = gpu.p1_fft_batch(vals, ns, doms, modes)
+    assert rc == 0
+    for c, out in zip(cases, outs):
+        ser = b"".join(oracle.serialize(out[144 * i:144 * i + 144]) for i in range(4096))
+        assert hashlib.sha256(ser).hexdigest() == c["sha256"], c["mode"]
+
+
+def test_fft_round_trip_2_16(gpu, oracle, synth):
+    """2^16 points (32768 butterflies per stage, one lane each): the inverse
+    of the forward transform is the identity."""
+    n = 1 << 16
+    aff = gpu.points_from_scalars(synth.point_scalars(72, n), n)
+    jac = oracle.jacobian_randomize(72, n, aff)
+    ok, d = gpu.fr_fft_domain_init(n)
+    ok1, f = gpu.p1_fft_with_domain(jac, n, d, n + 2, False)
+    ok2, b = gpu.p1_fft_with_domain(f, n, d, n + 2, True)
+    assert ok and ok1 and ok2
+    assert f != jac
+    for i in range(0, n, 7):
+        assert oracle.compress(b[144 * i:144 * i + 144]) == oracle.compress(jac[144 * i:144 * i + 144]), i
+
+
 def test_fft_batch_rejects_before_writing(gpu, oracle):
     n = 8
     jac = oracle.jacobian_randomize(9, n, oracle.gen_points(9, n))
