@@ -236,6 +236,31 @@ def test_msm_hot_buckets(gpu, oracle, synth):
     assert oracle.compress(gpu.p1s_mult_pippenger(pts, sc, n, 255)) == oracle.msm(pts, sc, n, 255)
 
 
+def test_msm_hot_buckets_segmented_block_join(gpu, oracle, synth):
+    """n = 2^22 with one scalar repeated and window 16: buckets average more
+    than two chunks (the segmented fixup), and each window's two occupied
+    buckets span ~50k chunks, so their joins take the block path of
+    k_fixup_hot_seg.  sum k P_i == (k sum s_i mod r) G."""
+    import numpy as np
+    import torch
+    n = 1 << 22
+    s = synth.point_scalars(4646, n)
+    k = synth.scalars(4747, 1, 0)
+    ks = torch.frombuffer(bytearray(s), dtype=torch.uint8).cuda()
+    dp = torch.empty(n * 96, dtype=torch.uint8, device="cuda")
+    torch.cuda.synchronize()
+    assert gpu.load().catmsm_p1_affines_from_scalars_device(dp.data_ptr(), ks.data_ptr(), n) == 0
+    del ks
+    dk = torch.frombuffer(bytearray(k * n), dtype=torch.uint8).cuda()
+    torch.cuda.synchronize()
+    got = oracle.compress(gpu.msm_device(dp.data_ptr(), dk.data_ptr(), 32, n, 255, 16))
+    sv = np.frombuffer(s, dtype=np.uint32).reshape(n, 8).astype(np.uint64)
+    ssum = sum(int(sv[:, i].sum()) << (32 * i) for i in range(8))
+    kk = int.from_bytes(k, "little")
+    exp = oracle.compress(oracle.mult(oracle.generator(), (kk * ssum % R).to_bytes(32, "little"), 256))
+    assert got == exp
+
+
 @pytest.mark.parametrize("glv", [0, 1])
 @pytest.mark.parametrize("window", [2, 5, 8, 13, 15, 16, 17, 20])
 def test_msm_device_windows(gpu, oracle, synth, window, glv):
