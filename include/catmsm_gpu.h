@@ -207,6 +207,19 @@ int catmsm_p1_fft_device(void *d_values, size_t n, const void *d_domain, int mod
 int catmsm_p1_fft_batch(blst_p1 *const values[], const size_t ns[], const blst_fr *const domains[],
                         const int modes[], size_t count);
 
+/* Forward G1 FFT of an input whose elements [xn, n) are the identity: the
+ * C-ABI form of the reference's fft_forward_truncated_prefix<G1Point, Fr,
+ * G1CoeffCtx> (blst/fft/ctFft.h:132-150, :384-460, :575-646; a C++ template
+ * there, used by the middle product, with no C entry of its own).  All n
+ * outputs equal blst_p1_fft_with_domain(values, n, domain, domain_len, false)
+ * on the same input; stage s runs only the butterflies of the min(xn, n / 2^s)
+ * groups that hold a non-identity input (the reference's plan).  Returns
+ * false before writing on: NULL values, an invalid size, domain length or
+ * tag (as blst_p1_fft_with_domain), xn == 0 or xn > n, or a non-identity
+ * element (z != 0) in [xn, n) (the reference leaves that case unspecified). */
+bool catmsm_p1_fft_truncated_prefix(blst_p1 *values, size_t n, size_t xn, const blst_fr *domain,
+                                    size_t domain_len);
+
 /* The calling thread's library CUDA stream (cudaStream_t), for event timing. */
 void *catmsm_stream(void);
 

@@ -173,6 +173,53 @@ bool oracle_p1_fft_with_domain(op1 *values, size_t n, const ofr *domain, size_t 
     return true;
 }
 
+/* ---- truncated-prefix forward transform (fft/ctFft.h:132-150 declaration,
+ * :384-460 make_fft_truncated_forward_plan, :575-646 the transform).  Inputs
+ * [xn, n) are the identity.  After the bit reversal a position is active iff
+ * it holds an input below xn; a butterfly runs iff either of its positions is
+ * active, and both are active afterwards.  The outputs equal the full forward
+ * transform (the reference's TruncatedForwardPrefixMatchesFullG1 test).  Like
+ * the reference, the identity tail is the caller's precondition. ---- */
+bool oracle_p1_fft_truncated_prefix(op1 *values, size_t n, size_t xn, const ofr *domain, size_t domain_len)
+{
+    if (!values || !domain_ok(n, domain, domain_len) || xn == 0 || xn > n) return false;
+    unsigned char *act = (unsigned char *)calloc(n, 1), *nxt = (unsigned char *)calloc(n, 1);
+    if (!act || !nxt) {
+        free(act);
+        free(nxt);
+        return false;
+    }
+    p1_bit_reverse(values, n);
+    for (size_t i = 0; i < n; i++) {
+        size_t r = 0;
+        for (size_t b = 1, m = n >> 1; b < n; b <<= 1, m >>= 1)
+            if (i & b) r |= m;
+        act[r] = i < xn;
+    }
+    for (size_t len = 2; len <= n; len <<= 1) {
+        size_t half = len / 2;
+        memset(nxt, 0, n);
+        for (size_t i = 0; i < n; i += len) {
+            for (size_t j = 0; j < half; j++) {
+                size_t l = i + j, r = l + half;
+                if (!act[l] && !act[r]) continue;
+                op1 u = values[l], t = values[r], nt;
+                if (j) p1_mult_fr(&t, &values[r], &domain[j * (n / len)]);
+                op1_dadd(&values[l], &u, &t);
+                op1_neg(&nt, &t);
+                op1_dadd(&values[r], &u, &nt);
+                nxt[l] = nxt[r] = 1;
+            }
+        }
+        unsigned char *tmp = act;
+        act = nxt;
+        nxt = tmp;
+    }
+    free(act);
+    free(nxt);
+    return true;
+}
+
 bool oracle_p1_ifft_unscaled_with_domain(op1 *values, size_t n, const ofr *domain, size_t domain_len)
 {
     if (!values || !domain_ok(n, domain, domain_len)) return false;

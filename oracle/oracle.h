@@ -107,6 +107,7 @@ bool oracle_fr_fft_domain_init(ofr *domain, size_t domain_len, size_t n);
 bool oracle_p1_fft(op1 *values, size_t n, bool inverse);
 bool oracle_p1_fft_with_domain(op1 *values, size_t n, const ofr *domain, size_t domain_len, bool inverse);
 bool oracle_p1_ifft_unscaled_with_domain(op1 *values, size_t n, const ofr *domain, size_t domain_len);
+bool oracle_p1_fft_truncated_prefix(op1 *values, size_t n, size_t xn, const ofr *domain, size_t domain_len);
 bool oracle_fr_fft(ofr *values, size_t n, bool inverse);
 bool oracle_fr_fft_with_domain(ofr *values, size_t n, const ofr *domain, size_t domain_len, bool inverse);
 void oracle_fr_root_of_unity(ofr *o, size_t log2n);

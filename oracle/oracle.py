@@ -142,6 +142,8 @@ class Oracle(_Common):
         L.oracle_p1_fft_with_domain.argtypes = [_vp, _sz, _vp, _sz, C.c_bool]
         L.oracle_p1_ifft_unscaled_with_domain.restype = C.c_bool
         L.oracle_p1_ifft_unscaled_with_domain.argtypes = [_vp, _sz, _vp, _sz]
+        L.oracle_p1_fft_truncated_prefix.restype = C.c_bool
+        L.oracle_p1_fft_truncated_prefix.argtypes = [_vp, _sz, _sz, _vp, _sz]
         L.oracle_fr_fft.restype = C.c_bool
         L.oracle_fr_fft.argtypes = [_vp, _sz, C.c_bool]
         L.oracle_fr_fft_with_domain.restype = C.c_bool
@@ -272,6 +274,11 @@ class Oracle(_Common):
     def p1_ifft_unscaled_with_domain(self, values, n, domain, domain_len):
         b = bytearray(values)
         ok = self.L.oracle_p1_ifft_unscaled_with_domain(_buf(b), n, _buf(domain), domain_len)
+        return ok, bytes(b)
+
+    def p1_fft_truncated_prefix(self, values, n, xn, domain, domain_len):
+        b = bytearray(values)
+        ok = self.L.oracle_p1_fft_truncated_prefix(_buf(b), n, xn, _buf(domain), domain_len)
         return ok, bytes(b)
 
     def fr_fft(self, values: bytes, n, inverse):

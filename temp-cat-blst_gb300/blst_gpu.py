@@ -76,6 +76,8 @@ def load(build_if_missing=True):
     L.catmsm_p1s_affine_in_g1.restype = C.c_int
     L.catmsm_p1s_affine_in_g1.argtypes = [_vp, _sz, _vp]
     L.catmsm_p1_fft_batch.restype = C.c_int
+    L.catmsm_p1_fft_truncated_prefix.restype = C.c_bool
+    L.catmsm_p1_fft_truncated_prefix.argtypes = [_vp, _sz, _sz, _vp, _sz]
     L.catmsm_p1_fft_batch.argtypes = [_vp, _vp, _vp, _vp, _sz]
     L.catmsm_stream.restype = _vp
     L.catmsm_stream.argtypes = []
@@ -281,6 +283,15 @@ def p1_ifft_unscaled_with_domain(values: bytes, n: int, domain: bytes, domain_le
     b = bytearray(values)
     ok = load().blst_p1_ifft_unscaled_with_domain(_buf(b) if b else None, n, _buf(domain) if domain else None,
                                                   domain_len)
+    return ok, bytes(b)
+
+
+def p1_fft_truncated_prefix(values: bytes, n: int, xn: int, domain: bytes, domain_len: int):
+    """Forward G1 FFT of values whose elements [xn, n) are the identity
+    (the reference's fft_forward_truncated_prefix); returns (ok, values)."""
+    b = bytearray(values)
+    ok = load().catmsm_p1_fft_truncated_prefix(_buf(b) if b else None, n, xn, _buf(domain) if domain else None,
+                                               domain_len)
     return ok, bytes(b)
 
 

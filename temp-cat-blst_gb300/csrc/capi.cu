@@ -125,7 +125,7 @@ static void msm_entry(blst_p1* ret, const blst_p1_affine* const points[], size_t
 
 // Common FFT driver.  domain == nullptr: one-shot (roots built from the
 // primitive root, or its inverse); else the caller's prepared domain.
-static bool fft_entry(blst_p1* values, size_t n, const blst_fr* domain, bool inverse, bool scaled)
+static bool fft_entry(blst_p1* values, size_t n, const blst_fr* domain, bool inverse, bool scaled, size_t xn = 0)
 {
     using namespace catmsm_host;
     Ctx* ctx = get_ctx();
@@ -157,7 +157,7 @@ static bool fft_entry(blst_p1* values, size_t n, const blst_fr* domain, bool inv
         }
     }
     if (err == cudaSuccess) err = cudaMemcpyAsync(dv, values, n * sizeof(blst_p1), cudaMemcpyHostToDevice, st);
-    if (err == cudaSuccess) err = fft_run(ctx, dv, n, dr, inv_from_fwd, scale);
+    if (err == cudaSuccess) err = fft_run(ctx, dv, n, dr, inv_from_fwd, scale, xn);
     // Results go to pinned staging first so a late failure leaves values untouched.
     void* hstage = nullptr;
     if (err == cudaSuccess) {
@@ -303,6 +303,21 @@ bool blst_p1_ifft_unscaled_with_domain(blst_p1* values, size_t n, const blst_fr*
     try {
         if (!values || !domain_tag_ok(n, domain, domain_len)) return false;
         return fft_entry(values, n, domain, true, false);
+    } catch (...) {
+        return false;
+    }
+}
+
+bool catmsm_p1_fft_truncated_prefix(blst_p1* values, size_t n, size_t xn, const blst_fr* domain,
+                                    size_t domain_len)
+{
+    try {
+        if (!values || !domain_tag_ok(n, domain, domain_len) || xn == 0 || xn > n) return false;
+        // the contract: every element of [xn, n) is the identity (z == 0)
+        static const uint8_t zero[sizeof(blst_fp)] = {0};
+        for (size_t i = xn; i < n; i++)
+            if (std::memcmp(&values[i].z, zero, sizeof(blst_fp)) != 0) return false;
+        return fft_entry(values, n, domain, false, false, xn);
     } catch (...) {
         return false;
     }

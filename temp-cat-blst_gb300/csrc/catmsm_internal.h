@@ -64,6 +64,7 @@ struct FftSpec {
     const uint32_t* roots_mont;
     bool inv_from_fwd;
     const uint32_t* scale_mont;
+    size_t xn = 0;          // forward transforms: inputs [xn, n) are the identity (0 = none known)
 };
 
 // Every transform of `specs` over the concatenated values in d_values.
@@ -74,7 +75,7 @@ cudaError_t fft_run_multi(Ctx* ctx, void* d_values, const FftSpec* specs, size_t
 // inv_from_fwd: read index n - j*(n/len) (inverse from forward roots);
 // d_scale_mont: optional Montgomery-form Fr applied to every output.
 cudaError_t fft_run(Ctx* ctx, void* d_values, size_t n, const uint32_t* d_roots_mont, bool inv_from_fwd,
-                    const uint32_t* d_scale_mont);
+                    const uint32_t* d_scale_mont, size_t xn = 0);
 
 // d_out[i] = w^i (Montgomery), i < n
 cudaError_t fft_root_powers(Ctx* ctx, const uint32_t* d_w_mont, size_t n, uint32_t* d_out);

@@ -84,6 +84,9 @@ struct FftJob {
     uint32_t glv_off;    // first prepared root (8 words each); glv_off + n: the scale
     int32_t inv_from_fwd;
     int32_t scaled;
+    uint32_t xn;         // inputs [xn, n) are the identity: stage s runs only the
+                         // min(xn, n / 2^s) groups holding a non-identity input
+    uint32_t pad;
 };
 
 // thread t of a launch over per-job ranges: find the job whose range holds t
@@ -132,7 +135,8 @@ __global__ void __launch_bounds__(64) k_fft_stage_multi(jac* __restrict__ a, con
     const uint32_t b = t - lst_pre[e];
     const uint32_t half = len >> 1;
     const uint32_t groups = J.n / len;
-    const uint32_t nontriv = groups * (half - 1);
+    const uint32_t active = min(groups, J.xn);
+    const uint32_t nontriv = active * (half - 1);
     uint32_t g, j;
     if (b < nontriv) {
         g = b / (half - 1);
@@ -141,6 +145,11 @@ __global__ void __launch_bounds__(64) k_fft_stage_multi(jac* __restrict__ a, con
         g = b - nontriv;
         j = 0;
     }
+    // After the bit-reversal permutation, position p holds input bitrev(p);
+    // group g of this stage (positions g len .. g len + len - 1) holds a
+    // non-identity input iff bitrev(g) over log2(groups) bits is below xn, so
+    // the active groups are the bit reversals of 0 .. active - 1.
+    if (active < groups) g = __brev(g) >> (32 - (J.logn - (31 - __clz(len))));
     jac* base = a + J.val_off;
     const uint32_t i0 = g * len + j, i1 = i0 + half;
     jac u, v;
@@ -238,6 +247,8 @@ cudaError_t fft_run_multi(Ctx* ctx, void* d_values, const FftSpec* specs, size_t
         jobs[i].inv_from_fwd = specs[i].inv_from_fwd ? 1 : 0;
         jobs[i].scaled = specs[i].scale_mont ? 1 : 0;
         jobs[i].glv_off = (uint32_t)glv_total;
+        jobs[i].xn = (uint32_t)(specs[i].xn && specs[i].xn < n ? specs[i].xn : n);
+        jobs[i].pad = 0;
         vpre[i] = (uint32_t)total;
         total += n;
         glv_total += n + 1;
@@ -255,7 +266,8 @@ cudaError_t fft_run_multi(Ctx* ctx, void* d_values, const FftSpec* specs, size_t
             if (jobs[i].logn >= s) {
                 lst_job.push_back((uint32_t)i);
                 lst_pre.push_back(acc);
-                acc += jobs[i].n / 2;
+                const uint32_t groups = jobs[i].n >> s;
+                acc += (groups < jobs[i].xn ? groups : jobs[i].xn) << (s - 1);
             }
         }
         st_cnt[s] = (uint32_t)lst_job.size() - st_off[s];
@@ -317,9 +329,9 @@ cudaError_t fft_run_multi(Ctx* ctx, void* d_values, const FftSpec* specs, size_t
 // single transform: d_values n Jacobian points; d_roots_mont the n
 // Montgomery roots the butterflies index; d_scale_mont optional scale
 cudaError_t fft_run(Ctx* ctx, void* d_values, size_t n, const uint32_t* d_roots_mont, bool inv_from_fwd,
-                    const uint32_t* d_scale_mont)
+                    const uint32_t* d_scale_mont, size_t xn)
 {
-    FftSpec sp{n, d_roots_mont, inv_from_fwd, d_scale_mont};
+    FftSpec sp{n, d_roots_mont, inv_from_fwd, d_scale_mont, xn};
     return fft_run_multi(ctx, d_values, &sp, 1);
 }
 

@@ -174,6 +174,56 @@ def test_fft_round_trip_2_16(gpu, oracle, synth):
         assert oracle.compress(b[144 * i:144 * i + 144]) == oracle.compress(jac[144 * i:144 * i + 144]), i
 
 
+def _padded(oracle, seed, n, xn):
+    jac = bytearray(oracle.jacobian_randomize(seed, n, oracle.gen_points(seed, n)))
+    jac[144 * xn:] = bytes(144 * (n - xn))
+    return bytes(jac)
+
+
+def test_fft_truncated_prefix_matches_oracle(gpu, oracle):
+    """catmsm_p1_fft_truncated_prefix against the oracle's restatement of the
+    reference's truncated-prefix plan (and so against the full transform),
+    bit for bit, over the reference test's xn and around powers of two."""
+    for n, xns in ((32, (1, 5, 13, 24, 32)), (1024, (1, 2, 3, 100, 511, 512, 513, 1000, 1024))):
+        d = oracle.domain(n)
+        for xn in xns:
+            jac = _padded(oracle, 300 + xn, n, xn)
+            ok, got = gpu.p1_fft_truncated_prefix(jac, n, xn, d, n + 2)
+            ok2, exp = oracle.p1_fft_truncated_prefix(jac, n, xn, d, n + 2)
+            assert ok and ok2
+            for i in range(n):
+                assert oracle.serialize(got[144 * i:144 * i + 144]) == oracle.serialize(exp[144 * i:144 * i + 144]), (n, xn, i)
+
+
+def test_fft_truncated_prefix_large_equals_full(gpu, oracle, synth):
+    """n = 2^16, xn = 5000: the early stages run only the active groups (quads
+    while they fit one wave, one lane per butterfly after); the outputs equal
+    the full forward transform of the same input."""
+    n, xn = 1 << 16, 5000
+    aff = gpu.points_from_scalars(synth.point_scalars(73, xn), xn)
+    jac = oracle.jacobian_randomize(73, xn, aff) + bytes(144 * (n - xn))
+    d = gpu.fr_fft_domain_init(n)[1]
+    ok, tr = gpu.p1_fft_truncated_prefix(jac, n, xn, d, n + 2)
+    ok2, full = gpu.p1_fft_with_domain(jac, n, d, n + 2, False)
+    assert ok and ok2
+    assert tr == full
+
+
+def test_fft_truncated_prefix_rejects_before_writing(gpu, oracle):
+    n = 16
+    d = oracle.domain(n)
+    jac = _padded(oracle, 333, n, 6)
+    for xn, dl in ((0, n + 2), (n + 1, n + 2), (6, n + 1)):
+        ok, out = gpu.p1_fft_truncated_prefix(jac, n, xn, d, dl)
+        assert not ok and out == jac
+    # a non-identity element past xn
+    ok, out = gpu.p1_fft_truncated_prefix(jac, n, 5, d, n + 2)
+    assert not ok and out == jac
+    ok, out = gpu.p1_fft_truncated_prefix(jac, 12, 6, d, n + 2)    # not a power of two
+    assert not ok and out == jac
+    assert gpu.p1_fft_truncated_prefix(jac, n, 6, d, n + 2)[0]
+
+
 def test_fft_batch_rejects_before_writing(gpu, oracle):
     n = 8
     jac = oracle.jacobian_randomize(9, n, oracle.gen_points(9, n))

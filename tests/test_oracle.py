@@ -265,3 +265,25 @@ def test_oracle_tile_matches_golden(golden, oracle):
     for c in cases:
         pts, sc = _msm_inputs(oracle, c)
         assert oracle.tile(pts, sc, c["n"], c["nbits"], c["bit0"], c["window"]).hex() == c["compressed"], c
+
+
+def test_oracle_fft_truncated_prefix_matches_full(oracle):
+    """The reference's TruncatedForwardPrefixMatchesFullG1 (test/Fft_tests.cpp:
+    974-1006) on the oracle: m = 32, xn in {1, 5, 13, 24, 32}, inputs [xn, m)
+    the identity; the truncated transform equals the full forward one."""
+    m = 32
+    d = oracle.domain(m)
+    for xn in (1, 5, 13, 24, 32):
+        jac = bytearray(oracle.jacobian_randomize(200 + xn, m, oracle.gen_points(200 + xn, m)))
+        jac[144 * xn:] = bytes(144 * (m - xn))
+        jac = bytes(jac)
+        ok1, full = oracle.p1_fft_with_domain(jac, m, d, m + 2, False)
+        ok2, tr = oracle.p1_fft_truncated_prefix(jac, m, xn, d, m + 2)
+        assert ok1 and ok2
+        for i in range(m):
+            assert oracle.serialize(full[144 * i:144 * i + 144]) == oracle.serialize(tr[144 * i:144 * i + 144]), xn
+    zero = bytes(144 * m)
+    assert not oracle.p1_fft_truncated_prefix(zero, m, 0, d, m + 2)[0]
+    assert not oracle.p1_fft_truncated_prefix(zero, m, m + 1, d, m + 2)[0]
+    assert not oracle.p1_fft_truncated_prefix(zero, m, 4, d, m + 1)[0]
+
