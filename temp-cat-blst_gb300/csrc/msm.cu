@@ -16,7 +16,8 @@
 //                    the scalar stages.
 //   1. k_digits      signed c-bit window digits (carry recoding, digit in
 //                    [-2^(c-1), 2^(c-1)]), one thread per scalar; each nonzero
-//                    digit takes a rank in its bucket with one atomicAdd.
+//                    digit takes a rank in its bucket (one atomicAdd per
+//                    bucket and warp).
 //   2. k_scan_*      exclusive scan of the D * 2^(c-1) bucket counts.
 //   3. k_scatter     counting-sort scatter of (point index | sign) into bucket
 //                    order, plus each entry's bucket key.
@@ -171,9 +172,11 @@ __global__ void k_digits(const uint8_t* __restrict__ scalars, uint32_t stride, u
                          uint32_t* __restrict__ ranks, uint32_t* __restrict__ counts)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    const bool valid = i < n;
     uint32_t k[9];
-    load_scalar(k, scalars + (size_t)i * stride, stride, nbits);
+    if (valid) load_scalar(k, scalars + (size_t)i * stride, stride, nbits);
+    else
+        for (int j = 0; j < 8; j++) k[j] = 0;
     k[8] = 0;
     const uint32_t B = 1u << (c - 1);
     const uint32_t cmask = (1u << c) - 1;
@@ -187,12 +190,14 @@ __global__ void k_digits(const uint8_t* __restrict__ scalars, uint32_t stride, u
         if (d > (int32_t)B) { d -= (int32_t)(cmask + 1); carry = 1; }
         else carry = 0;
         const size_t o = (size_t)w * n + i;
+        const uint32_t mag = d < 0 ? (uint32_t)(-d) : (uint32_t)d;
+        const uint32_t key = (valid && d != 0) ? w * B + (mag - 1) : kNoBucket;
+        const uint32_t rank = warp_bucket_rank(key, counts);
+        if (!valid) continue;
         if (d == 0) {
             digits[o] = 0xffffffffu;
         } else {
-            const uint32_t mag = d < 0 ? (uint32_t)(-d) : (uint32_t)d;
-            const uint32_t key = w * B + (mag - 1);
-            ranks[o] = atomicAdd(&counts[key], 1u);
+            ranks[o] = rank;
             digits[o] = key | (d < 0 ? 0x80000000u : 0u);
         }
     }
@@ -208,9 +213,11 @@ __global__ void k_tile_digits(const uint8_t* __restrict__ scalars, uint32_t stri
                               uint32_t* __restrict__ ranks, uint32_t* __restrict__ counts)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    const bool valid = i < n;
     uint32_t k[9];
-    load_scalar(k, scalars + (size_t)i * stride, stride, nbits);
+    if (valid) load_scalar(k, scalars + (size_t)i * stride, stride, nbits);
+    else
+        for (int j = 0; j < 8; j++) k[j] = 0;
     k[8] = 0;
     const uint32_t begin = bit0 > 0 ? bit0 - 1 : 0;
     const uint32_t endb = min(bit0 + window, nbits);
@@ -223,12 +230,14 @@ __global__ void k_tile_digits(const uint8_t* __restrict__ scalars, uint32_t stri
     const uint32_t sign = (v >> enc) & 1;
     const uint32_t val = (v + 1) >> 1;
     const uint32_t mag = sign ? (1u << enc) - val : val;
+    const uint32_t key = (valid && mag != 0) ? mag - 1 : kNoBucket;
+    const uint32_t rank = warp_bucket_rank(key, counts);
+    if (!valid) return;
     if (mag == 0) {
         digits[i] = 0xffffffffu;
         return;
     }
-    const uint32_t key = mag - 1;
-    ranks[i] = atomicAdd(&counts[key], 1u);
+    ranks[i] = rank;
     digits[i] = key | (sign ? 0x80000000u : 0u);
 }
 
