@@ -397,7 +397,7 @@ __global__ void __launch_bounds__(128) k_fixup(const uint32_t* __restrict__ sort
                                                const uint32_t* __restrict__ total_ptr, uint32_t L,
                                                xyzz* __restrict__ buckets, const xyzz* __restrict__ head,
                                                const xyzz* __restrict__ tail, uint2* __restrict__ hot_list,
-                                               uint32_t* __restrict__ hot_count)
+                                               uint32_t* __restrict__ hot_count, uint32_t cap)
 {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t E = *total_ptr;
@@ -417,11 +417,38 @@ __global__ void __launch_bounds__(128) k_fixup(const uint32_t* __restrict__ sort
     }
     xyzz acc, part;
     load_xyzz(acc, tail + t);
-    for (uint32_t u = t + 1; u <= t1; u++) {
-        load_xyzz(part, head + u);
-        xyzz_add(acc, part);
-    }
+    load_xyzz(part, head + t + 1);
+    xyzz_add(acc, part);
     store_xyzz(buckets + last, acc);
+    if (t1 > t + 1) {
+        // the rest of a 3..kHotSpan-chunk bucket: k_fixup_rest, so the
+        // warp's other lanes do not wait through a second addition
+        const uint32_t h = atomicAdd(hot_count + 1, 1u);
+        hot_list[cap - 1 - h] = make_uint2(last, t);
+    }
+}
+
+// Finishes the buckets k_fixup left after their first join (list at the top
+// of the hot-list buffer, count hot_count[1]): heads t0 + 2 .. t1, one
+// thread per bucket, grid-stride.
+__global__ void __launch_bounds__(128) k_fixup_rest(const uint2* __restrict__ hot_list,
+                                                    const uint32_t* __restrict__ hot_count, uint32_t cap,
+                                                    const uint32_t* __restrict__ offsets, uint32_t L,
+                                                    xyzz* __restrict__ buckets, const xyzz* __restrict__ head)
+{
+    const uint32_t nr = hot_count[1];
+    for (uint32_t h = blockIdx.x * blockDim.x + threadIdx.x; h < nr; h += gridDim.x * blockDim.x) {
+        const uint2 e = hot_list[cap - 1 - h];
+        const uint32_t key = e.x, t0 = e.y;
+        const uint32_t t1 = (offsets[key + 1] - 1) / L;
+        xyzz acc, part;
+        load_xyzz(acc, buckets + key);
+        for (uint32_t u = t0 + 2; u <= t1; u++) {
+            load_xyzz(part, head + u);
+            xyzz_add(acc, part);
+        }
+        store_xyzz(buckets + key, acc);
+    }
 }
 
 __device__ __forceinline__ void shfl_down_xyzz(xyzz& o, const xyzz& v, int d)
@@ -1010,7 +1037,7 @@ static cudaError_t msm_run(Ctx* ctx, const void* d_points, const uint8_t* d_scal
 
     CATMSM_CHECK(cudaMemsetAsync(counts, 0, M * 4, st));
     CATMSM_CHECK(cudaMemsetAsync(buckets, 0, M * sizeof(xyzz), st));
-    CATMSM_CHECK(cudaMemsetAsync(hot_count, 0, 4, st));
+    CATMSM_CHECK(cudaMemsetAsync(hot_count, 0, 8, st));   // hot list and rest list counts
     mark(1);
     if (tile_window)
         k_tile_digits<<<div_up(n, 256), 256, 0, st>>>(d_scalars, stride, (uint32_t)n, nbits, tile_bit0, tile_window, c,
@@ -1044,8 +1071,10 @@ static cudaError_t msm_run(Ctx* ctx, const void* d_points, const uint8_t* d_scal
     } else {
         // short spans: one thread joins each bucket's few carries
         k_fixup<<<div_up(chunks, 128), 128, 0, st>>>(sorted_key, offsets, total, L, buckets, head, tail, hot_list,
-                                                     hot_count);
+                                                     hot_count, (uint32_t)chunks);
         k_fixup_hot<<<2 * kSMs, kHotThreads, 0, st>>>(hot_list, hot_count, offsets, L, buckets, head, tail);
+        k_fixup_rest<<<2 * kSMs, 128, 0, st>>>(hot_list, hot_count, (uint32_t)chunks, offsets, L, buckets, head);
+        g_stats.launches++;
     }
     mark(6);
     {

@@ -52,7 +52,10 @@ __global__ void k_accumulate(const affine* __restrict__ pts, const uint32_t* __r
 __global__ void k_fixup(const uint32_t* __restrict__ sorted_key, const uint32_t* __restrict__ offsets,
                         const uint32_t* __restrict__ total_ptr, uint32_t L, xyzz* __restrict__ buckets,
                         const xyzz* __restrict__ head, const xyzz* __restrict__ tail,
-                        uint2* __restrict__ hot_list, uint32_t* __restrict__ hot_count);
+                        uint2* __restrict__ hot_list, uint32_t* __restrict__ hot_count, uint32_t cap);
+__global__ void k_fixup_rest(const uint2* __restrict__ hot_list, const uint32_t* __restrict__ hot_count,
+                             uint32_t cap, const uint32_t* __restrict__ offsets, uint32_t L,
+                             xyzz* __restrict__ buckets, const xyzz* __restrict__ head);
 __global__ void k_fixup_hot(const uint2* __restrict__ hot_list, const uint32_t* __restrict__ hot_count,
                             const uint32_t* __restrict__ offsets, uint32_t L, xyzz* __restrict__ buckets,
                             const xyzz* __restrict__ head, const xyzz* __restrict__ tail);
@@ -155,7 +158,7 @@ static cudaError_t noalloc_run(const blst_p1_affine* points, const blst_byte* sc
     // regions read before they are written in this call start at zero
     CATMSM_CHECK(cudaMemsetAsync(counts, 0, M * 4, st));
     CATMSM_CHECK(cudaMemsetAsync(buckets, 0, M * sizeof(xyzz), st));
-    CATMSM_CHECK(cudaMemsetAsync(hot_count, 0, 4, st));
+    CATMSM_CHECK(cudaMemsetAsync(hot_count, 0, 8, st));
     k_digits<<<div_up(n, 256), 256, 0, st>>>(d_sc, nbytes, (uint32_t)n, nbits, kC, D, digits, ranks, counts);
     k_scan_local<<<nblocks, 1024, 0, st>>>(counts, offsets, bsums, (uint32_t)M);
     k_scan_top<<<1, 1024, 0, st>>>(bsums, nblocks, total);
@@ -164,8 +167,9 @@ static cudaError_t noalloc_run(const blst_p1_affine* points, const blst_byte* sc
                                               sorted_key);
     k_accumulate<<<div_up(chunks, 128), 128, 0, st>>>(d_pts, sorted_pt, sorted_key, total, kL, buckets, head, tail);
     k_fixup<<<div_up(chunks, 128), 128, 0, st>>>(sorted_key, offsets, total, kL, buckets, head, tail, hot_list,
-                                                 hot_count);
+                                                 hot_count, (uint32_t)kChunks);
     k_fixup_hot<<<kSMs, 128, 0, st>>>(hot_list, hot_count, offsets, kL, buckets, head, tail);
+    k_fixup_rest<<<kSMs, 128, 0, st>>>(hot_list, hot_count, (uint32_t)kChunks, offsets, kL, buckets, head);
     xyzz* bufA[2] = {seg, seg + 2 * kLvl1};
     xyzz* bufQ[2] = {seg + kLvl1, seg + 2 * kLvl1 + kLvl2};
     const xyzz* inA = buckets;
