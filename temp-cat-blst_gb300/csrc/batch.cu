@@ -132,19 +132,16 @@ __global__ void k_digits_batch(const uint8_t* __restrict__ scalars, const uint32
 {
     const uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t P = off[nmsm];
-    const bool valid = f < P && f < cap;
+    if (f >= P || f >= cap) return;
     uint32_t lo = 0, hi = nmsm;                   // find j with off[j] <= f < off[j+1]
-    while (valid && hi - lo > 1) {
+    while (hi - lo > 1) {
         const uint32_t mid = (lo + hi) >> 1;
         if (off[mid] <= f) lo = mid;
         else hi = mid;
     }
-    const uint32_t j = lo, i = valid ? f - off[j] : 0;
-    uint4 a = make_uint4(0, 0, 0, 0), b = a;
-    if (valid) {
-        a = __ldg(reinterpret_cast<const uint4*>(scalars + (size_t)f * 32));
-        b = __ldg(reinterpret_cast<const uint4*>(scalars + (size_t)f * 32) + 1);
-    }
+    const uint32_t j = lo, i = f - off[j];
+    const uint4 a = __ldg(reinterpret_cast<const uint4*>(scalars + (size_t)f * 32));
+    const uint4 b = __ldg(reinterpret_cast<const uint4*>(scalars + (size_t)f * 32) + 1);
     uint32_t k[9] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, 0};
 #pragma unroll
     for (uint32_t q = 0; q < 8; q++) {
@@ -163,14 +160,14 @@ __global__ void k_digits_batch(const uint8_t* __restrict__ scalars, const uint32
         if (d > (int32_t)B) { d -= (int32_t)(cmask + 1); carry = 1; }
         else carry = 0;
         const size_t o = (size_t)f * D + w;
-        const uint32_t mag = d < 0 ? (uint32_t)(-d) : (uint32_t)d;
-        const uint32_t key = (valid && d != 0) ? j * B + (mag - 1) : kNoBucket;
-        const uint32_t rank = warp_bucket_rank(key, counts);
-        if (!valid) continue;
         if (d == 0) {
             digits[o] = 0xffffffffu;
         } else {
-            ranks[o] = rank;
+            // plain atomics: an MSM of the batch has at most n points per
+            // bucket, and warp aggregation cost more than it saved here
+            const uint32_t mag = d < 0 ? (uint32_t)(-d) : (uint32_t)d;
+            const uint32_t key = j * B + (mag - 1);
+            ranks[o] = atomicAdd(&counts[key], 1u);
             digits[o] = key | (d < 0 ? 0x80000000u : 0u);
             pidx[o] = w * n + i;
         }
