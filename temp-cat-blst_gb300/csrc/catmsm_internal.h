@@ -33,6 +33,10 @@ cudaError_t msm_setup_device();
 // pairs (m <= msm_reduce_tail_max(D)); roots to outQ[0..D).
 uint32_t msm_reduce_tail_max(uint32_t D);
 void msm_reduce_tail(const void* inA, const void* inQ, uint32_t m, uint32_t D, void* outQ, cudaStream_t st);
+// Joins of buckets whose carries span more than 1024 partials, by the whole
+// grid (after k_fixup_hot / k_fixup_hot_seg; seg = the segmented fixup).
+void fixup_giants(const void* hot_list, const uint32_t* hot_count, const uint32_t* offsets, uint32_t L,
+                  void* buckets, void* head, void* tail, bool seg, cudaStream_t st);
 // One binary reduction level (fan-in 2) over D sets of m (A, Q) pairs.
 void msm_reduce_pair(const void* inA, const void* inQ, uint32_t m, uint32_t D, void* outA, void* outQ,
                      cudaStream_t st);

@@ -487,6 +487,8 @@ __device__ __forceinline__ void warp_join(xyzz& acc, uint32_t span, uint32_t lan
 // repeated scalar): the whole block, span / blockDim additions per thread,
 // then a tree over lanes and over the block's warps.  Thread 0 gets the sum.
 constexpr uint32_t kWarpJoinMax = 160;   // larger spans are joined by a block
+constexpr uint32_t kGiantMin = 1024;     // larger spans are joined by the grid (k_fixup_giant)
+constexpr uint32_t kGiantSlice = 256;
 
 template <class PartAt>
 __device__ __forceinline__ void block_join(xyzz& acc, uint32_t span, PartAt part_at, xyzz* sh)
@@ -533,7 +535,7 @@ __global__ void __launch_bounds__(kHotThreads) k_fixup_hot(const uint2* __restri
         const uint2 e = hot_list[h];
         const uint32_t key = e.x, t0 = e.y;
         const uint32_t span = (offsets[key + 1] - 1) / L - t0 + 1;
-        if (span <= kWarpJoinMax) continue;
+        if (span <= kWarpJoinMax || span > kGiantMin) continue;        // giants: k_fixup_giant
         xyzz acc;
         block_join(acc, span, [&](uint32_t i) { return i == 0 ? tail + t0 : head + t0 + i; }, sh);
         if (threadIdx.x == 0) store_xyzz(buckets + key, acc);
@@ -643,10 +645,96 @@ __global__ void __launch_bounds__(kHotThreads) k_fixup_hot_seg(const uint2* __re
         const uint32_t key = e.x, t0 = e.y;
         const uint32_t t1 = (offsets[key + 1] - 1) / L;
         const uint32_t np = 2 + (t1 >> 5) - ((t0 + 1) >> 5);
-        if (np <= kWarpJoinMax) continue;
+        if (np <= kWarpJoinMax || np > kGiantMin) continue;            // giants: k_fixup_giant
         xyzz acc;
         block_join(acc, np, [&](uint32_t i) { return piece(t0, i); }, sh);
         if (threadIdx.x == 0) store_xyzz(buckets + key, acc);
+    }
+}
+
+// Buckets of more than kGiantMin partials (all-equal scalars, a forced narrow
+// top window) are joined by the whole grid instead of one block: every block
+// reduces kGiantSlice-partial slices and writes each slice's sum over the
+// slice's first partial (k_fixup_giant), then one block per bucket joins the
+// slice sums (k_fixup_giant_join).  The slices of all giants are dealt to
+// the blocks round-robin.  A bucket of 2^20 entries (~14k chunks) costs
+// ~2 + 7 + 7 dependent additions instead of span / 128 + 7.  Seg: the pieces k_fixup_seg
+// left, as in k_fixup_hot_seg; otherwise tail[t0] and head[t0 + 1 .. t1].
+template <bool Seg>
+__device__ __forceinline__ xyzz* hot_part(xyzz* head, xyzz* tail, uint32_t t0, uint32_t i)
+{
+    if (i == 0) return tail + t0;
+    if (!Seg || i == 1) return head + t0 + i;
+    return head + (((t0 + 1) | 31u) + 1 + 32 * (i - 2));
+}
+
+template <bool Seg>
+__device__ __forceinline__ uint32_t hot_parts(uint32_t key, uint32_t t0, const uint32_t* offsets, uint32_t L)
+{
+    const uint32_t t1 = (offsets[key + 1] - 1) / L;
+    return Seg ? 2 + (t1 >> 5) - ((t0 + 1) >> 5) : t1 - t0 + 1;
+}
+
+template <bool Seg>
+__global__ void __launch_bounds__(kHotThreads) k_fixup_giant(const uint2* __restrict__ hot_list,
+                                                             const uint32_t* __restrict__ hot_count,
+                                                             const uint32_t* __restrict__ offsets, uint32_t L,
+                                                             xyzz* __restrict__ head, xyzz* __restrict__ tail)
+{
+    __shared__ xyzz sh[kHotThreads / 32];
+    const uint32_t nh = *hot_count;
+    uint32_t base = 0;                      // slices of the giants before this one
+    for (uint32_t h = 0; h < nh; h++) {
+        const uint2 e = hot_list[h];
+        const uint32_t np = hot_parts<Seg>(e.x, e.y, offsets, L);
+        if (np <= kGiantMin) continue;
+        const uint32_t ns = (np + kGiantSlice - 1) / kGiantSlice;
+        // global slice base + sl goes to block (base + sl) mod gridDim.x, so
+        // the slices of every giant run at once
+        const uint32_t first = (blockIdx.x + gridDim.x - base % gridDim.x) % gridDim.x;
+        base += ns;
+        for (uint32_t sl = first; sl < ns; sl += gridDim.x) {
+            const uint32_t b0 = sl * kGiantSlice;
+            xyzz acc;
+            block_join(acc, min(kGiantSlice, np - b0), [&](uint32_t i) { return hot_part<Seg>(head, tail, e.y, b0 + i); },
+                       sh);
+            if (threadIdx.x == 0) store_xyzz(hot_part<Seg>(head, tail, e.y, b0), acc);
+        }
+    }
+}
+
+template <bool Seg>
+__global__ void __launch_bounds__(kHotThreads) k_fixup_giant_join(const uint2* __restrict__ hot_list,
+                                                                  const uint32_t* __restrict__ hot_count,
+                                                                  const uint32_t* __restrict__ offsets, uint32_t L,
+                                                                  xyzz* __restrict__ buckets, xyzz* __restrict__ head,
+                                                                  xyzz* __restrict__ tail)
+{
+    __shared__ xyzz sh[kHotThreads / 32];
+    const uint32_t nh = *hot_count;
+    for (uint32_t h = blockIdx.x; h < nh; h += gridDim.x) {
+        const uint2 e = hot_list[h];
+        const uint32_t np = hot_parts<Seg>(e.x, e.y, offsets, L);
+        if (np <= kGiantMin) continue;
+        const uint32_t ns = (np + kGiantSlice - 1) / kGiantSlice;
+        xyzz acc;
+        block_join(acc, ns, [&](uint32_t sl) { return hot_part<Seg>(head, tail, e.y, sl * kGiantSlice); }, sh);
+        if (threadIdx.x == 0) store_xyzz(buckets + e.x, acc);
+    }
+}
+
+void fixup_giants(const void* hot_list, const uint32_t* hot_count, const uint32_t* offsets, uint32_t L,
+                  void* buckets, void* head, void* tail, bool seg, cudaStream_t st)
+{
+    const uint2* hl = (const uint2*)hot_list;
+    if (seg) {
+        k_fixup_giant<true><<<2 * kSMs, kHotThreads, 0, st>>>(hl, hot_count, offsets, L, (xyzz*)head, (xyzz*)tail);
+        k_fixup_giant_join<true><<<2 * kSMs, kHotThreads, 0, st>>>(hl, hot_count, offsets, L, (xyzz*)buckets,
+                                                                   (xyzz*)head, (xyzz*)tail);
+    } else {
+        k_fixup_giant<false><<<2 * kSMs, kHotThreads, 0, st>>>(hl, hot_count, offsets, L, (xyzz*)head, (xyzz*)tail);
+        k_fixup_giant_join<false><<<2 * kSMs, kHotThreads, 0, st>>>(hl, hot_count, offsets, L, (xyzz*)buckets,
+                                                                    (xyzz*)head, (xyzz*)tail);
     }
 }
 
@@ -1067,14 +1155,16 @@ static cudaError_t msm_run(Ctx* ctx, const void* d_points, const uint8_t* d_scal
         k_fixup_join<<<div_up(chunks, 128), 128, 0, st>>>(sorted_key, offsets, total, L, buckets, head, tail,
                                                           hot_list, hot_count);
         k_fixup_hot_seg<<<2 * kSMs, kHotThreads, 0, st>>>(hot_list, hot_count, offsets, L, buckets, head, tail);
-        g_stats.launches++;
+        fixup_giants(hot_list, hot_count, offsets, L, buckets, head, tail, true, st);
+        g_stats.launches += 3;
     } else {
         // short spans: one thread joins each bucket's few carries
         k_fixup<<<div_up(chunks, 128), 128, 0, st>>>(sorted_key, offsets, total, L, buckets, head, tail, hot_list,
                                                      hot_count, (uint32_t)chunks);
         k_fixup_hot<<<2 * kSMs, kHotThreads, 0, st>>>(hot_list, hot_count, offsets, L, buckets, head, tail);
         k_fixup_rest<<<2 * kSMs, 128, 0, st>>>(hot_list, hot_count, (uint32_t)chunks, offsets, L, buckets, head);
-        g_stats.launches++;
+        fixup_giants(hot_list, hot_count, offsets, L, buckets, head, tail, false, st);
+        g_stats.launches += 3;
     }
     mark(6);
     {

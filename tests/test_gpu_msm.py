@@ -228,7 +228,8 @@ def test_msm_linearity_max_size(gpu, oracle, synth):
 
 def test_msm_hot_buckets(gpu, oracle, synth):
     """Every window puts all points in one bucket (equal scalars): the
-    chunk-spanning fixup must stay parallel and exact."""
+    chunk-spanning fixup must stay parallel and exact (spans of ~1.9k
+    chunks: the grid-wide join of the serial fixup, k_fixup_giant<false>)."""
     n = 1 << 16
     pts = oracle.gen_points(31, n)
     k = synth.scalars(32, 1, 0)
@@ -236,11 +237,11 @@ def test_msm_hot_buckets(gpu, oracle, synth):
     assert oracle.compress(gpu.p1s_mult_pippenger(pts, sc, n, 255)) == oracle.msm(pts, sc, n, 255)
 
 
-def test_msm_hot_buckets_segmented_block_join(gpu, oracle, synth):
+def test_msm_hot_buckets_segmented_grid_join(gpu, oracle, synth):
     """n = 2^22 with one scalar repeated and window 16: buckets average more
     than two chunks (the segmented fixup), and each window's two occupied
-    buckets span ~50k chunks, so their joins take the block path of
-    k_fixup_hot_seg.  sum k P_i == (k sum s_i mod r) G."""
+    buckets span ~44k chunks (~1.4k warp pieces), so their joins take the
+    grid-wide path (k_fixup_giant<true>).  sum k P_i == (k sum s_i mod r) G."""
     import numpy as np
     import torch
     n = 1 << 22
