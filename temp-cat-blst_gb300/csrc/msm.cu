@@ -384,11 +384,12 @@ __global__ void __launch_bounds__(128, 4) k_accumulate(const affine* __restrict_
 
 // ----------------------------------------------------------------- 5. fixup
 // A bucket whose entries cross chunk edges has partial sums in tail[t0]
-// (its first chunk) and head[t0+1 .. t1].  Short spans are joined by one
-// thread; spans longer than kHotSpan chunks (the narrow top window's
-// buckets, repeated scalars) go to a list that k_fixup_hot reduces with one
-// warp per bucket and a tree as deep as the span, so no serial chain is
-// longer than kHotSpan additions.
+// (its first chunk) and head[t0+1 .. t1].  Spans of up to kHotSpan chunks
+// are joined by one thread (k_fixup: the first join; k_fixup_rest: the rest
+// of 3..kHotSpan-chunk spans).  Longer spans (the narrow top window's
+// buckets, repeated scalars) go to a hot list joined by one warp (up to
+// kWarpJoinMax partials), one block (up to kGiantMin) or the whole grid
+// (k_fixup_giant), so no serial chain grows with the span.
 constexpr uint32_t kHotSpan = 4;
 constexpr int kHotThreads = 128;
 
@@ -459,9 +460,8 @@ __device__ __forceinline__ void shfl_down_xyzz(xyzz& o, const xyzz& v, int d)
     for (int k = 0; k < 48; k++) po[k] = __shfl_down_sync(0xffffffffu, pv[k], d);
 }
 
-// Sum of `span` partials of one bucket by one warp.
-// The warp's eight quads each add every 8th partial with quad point
-// operations, then a tree over the quads as deep as the span needs: a span
+// Sum of `span` partials of one bucket by one warp: the warp's eight quads
+// each add every 8th partial with quad point operations, then a tree over the quads as deep as the span needs: a span
 // of s <= 8 costs 1 + ceil(log2 s) quad additions (~10k cycles each against
 // ~26k for one lane's addition).  Lane 0 ends with the sum.
 template <class PartAt>
