@@ -46,7 +46,7 @@ __global__ void k_fixup(const uint32_t* __restrict__ sorted_key, const uint32_t*
                         const uint32_t* __restrict__ total_ptr, uint32_t L, xyzz* __restrict__ buckets,
                         const xyzz* __restrict__ head, const xyzz* __restrict__ tail,
                         uint2* __restrict__ hot_list, uint32_t* __restrict__ hot_count);
-__global__ void k_fixup_hot(const uint2* __restrict__ hot_list, const uint32_t* __restrict__ hot_count,
+__global__ void k_fixup_hot(uint2* __restrict__ hot_list, uint32_t* __restrict__ hot_count,
                             const uint32_t* __restrict__ offsets, uint32_t L, xyzz* __restrict__ buckets,
                             const xyzz* __restrict__ head, const xyzz* __restrict__ tail);
 __global__ void k_fixup_seg(const uint32_t* __restrict__ sorted_key, const uint32_t* __restrict__ total_ptr,
@@ -55,7 +55,7 @@ __global__ void k_fixup_join(const uint32_t* __restrict__ sorted_key, const uint
                              const uint32_t* __restrict__ total_ptr, uint32_t L, xyzz* __restrict__ buckets,
                              const xyzz* __restrict__ head, const xyzz* __restrict__ tail,
                              uint2* __restrict__ hot_list, uint32_t* __restrict__ hot_count);
-__global__ void k_fixup_hot_seg(const uint2* __restrict__ hot_list, const uint32_t* __restrict__ hot_count,
+__global__ void k_fixup_hot_seg(uint2* __restrict__ hot_list, uint32_t* __restrict__ hot_count,
                                 const uint32_t* __restrict__ offsets, uint32_t L, xyzz* __restrict__ buckets,
                                 const xyzz* __restrict__ head, const xyzz* __restrict__ tail);
 __global__ void k_reduce_level(const xyzz* __restrict__ inA, const xyzz* __restrict__ inQ, uint32_t m_in,
@@ -311,7 +311,7 @@ static uint32_t enqueue_batch(const Basis* b, BatchWork* w, cudaStream_t st, uin
     xyzz* seg = (xyzz*)w->seg.p;
     cudaMemsetAsync(counts, 0, M * 4, st);
     cudaMemsetAsync(buckets, 0, M * sizeof(xyzz), st);
-    cudaMemsetAsync(hot_count, 0, 4, st);
+    cudaMemsetAsync(hot_count, 0, 12, st);
     k_digits_batch<<<div_up(cap, 256), 256, 0, st>>>((const uint8_t*)w->scal.p, off, nmsm, (uint32_t)b->n, 256, c,
                                                     D, (uint32_t)cap, (uint32_t*)w->digits.p,
                                                     (uint32_t*)w->ranks.p, (uint32_t*)w->pidx.p, counts);

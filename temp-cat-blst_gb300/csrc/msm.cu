@@ -512,8 +512,8 @@ __device__ __forceinline__ void block_join(xyzz& acc, uint32_t span, PartAt part
         for (uint32_t w = 1; w < blockDim.x / 32; w++) xyzz_add(acc, sh[w]);
 }
 
-__global__ void __launch_bounds__(kHotThreads) k_fixup_hot(const uint2* __restrict__ hot_list,
-                                                           const uint32_t* __restrict__ hot_count,
+__global__ void __launch_bounds__(kHotThreads) k_fixup_hot(uint2* __restrict__ hot_list,
+                                                           uint32_t* __restrict__ hot_count,
                                                            const uint32_t* __restrict__ offsets, uint32_t L,
                                                            xyzz* __restrict__ buckets, const xyzz* __restrict__ head,
                                                            const xyzz* __restrict__ tail)
@@ -535,7 +535,11 @@ __global__ void __launch_bounds__(kHotThreads) k_fixup_hot(const uint2* __restri
         const uint2 e = hot_list[h];
         const uint32_t key = e.x, t0 = e.y;
         const uint32_t span = (offsets[key + 1] - 1) / L - t0 + 1;
-        if (span <= kWarpJoinMax || span > kGiantMin) continue;        // giants: k_fixup_giant
+        if (span <= kWarpJoinMax) continue;
+        if (span > kGiantMin) {                                        // joined by the grid: the giant list
+            if (threadIdx.x == 0) hot_list[nh + atomicAdd(hot_count + 2, 1u)] = e;
+            continue;
+        }
         xyzz acc;
         block_join(acc, span, [&](uint32_t i) { return i == 0 ? tail + t0 : head + t0 + i; }, sh);
         if (threadIdx.x == 0) store_xyzz(buckets + key, acc);
@@ -616,8 +620,8 @@ __global__ void __launch_bounds__(128) k_fixup_join(const uint32_t* __restrict__
 
 // k_fixup_hot over the pieces k_fixup_seg left: tail[t0], head[t0 + 1] and
 // the head slot at each later warp boundary up to t1.
-__global__ void __launch_bounds__(kHotThreads) k_fixup_hot_seg(const uint2* __restrict__ hot_list,
-                                                               const uint32_t* __restrict__ hot_count,
+__global__ void __launch_bounds__(kHotThreads) k_fixup_hot_seg(uint2* __restrict__ hot_list,
+                                                               uint32_t* __restrict__ hot_count,
                                                                const uint32_t* __restrict__ offsets, uint32_t L,
                                                                xyzz* __restrict__ buckets,
                                                                const xyzz* __restrict__ head,
@@ -645,7 +649,11 @@ __global__ void __launch_bounds__(kHotThreads) k_fixup_hot_seg(const uint2* __re
         const uint32_t key = e.x, t0 = e.y;
         const uint32_t t1 = (offsets[key + 1] - 1) / L;
         const uint32_t np = 2 + (t1 >> 5) - ((t0 + 1) >> 5);
-        if (np <= kWarpJoinMax || np > kGiantMin) continue;            // giants: k_fixup_giant
+        if (np <= kWarpJoinMax) continue;
+        if (np > kGiantMin) {                                          // joined by the grid: the giant list
+            if (threadIdx.x == 0) hot_list[nh + atomicAdd(hot_count + 2, 1u)] = e;
+            continue;
+        }
         xyzz acc;
         block_join(acc, np, [&](uint32_t i) { return piece(t0, i); }, sh);
         if (threadIdx.x == 0) store_xyzz(buckets + key, acc);
@@ -653,7 +661,8 @@ __global__ void __launch_bounds__(kHotThreads) k_fixup_hot_seg(const uint2* __re
 }
 
 // Buckets of more than kGiantMin partials (all-equal scalars, a forced narrow
-// top window) are joined by the whole grid instead of one block: every block
+// top window; k_fixup_hot / k_fixup_hot_seg list them after the hot list,
+// count hot_count[2]) are joined by the whole grid instead of one block: every block
 // reduces kGiantSlice-partial slices and writes each slice's sum over the
 // slice's first partial (k_fixup_giant), then one block per bucket joins the
 // slice sums (k_fixup_giant_join).  The slices of all giants are dealt to
@@ -682,10 +691,11 @@ __global__ void __launch_bounds__(kHotThreads) k_fixup_giant(const uint2* __rest
                                                              xyzz* __restrict__ head, xyzz* __restrict__ tail)
 {
     __shared__ xyzz sh[kHotThreads / 32];
-    const uint32_t nh = *hot_count;
+    const uint2* giants = hot_list + hot_count[0];
+    const uint32_t ng = hot_count[2];
     uint32_t base = 0;                      // slices of the giants before this one
-    for (uint32_t h = 0; h < nh; h++) {
-        const uint2 e = hot_list[h];
+    for (uint32_t h = 0; h < ng; h++) {
+        const uint2 e = giants[h];
         const uint32_t np = hot_parts<Seg>(e.x, e.y, offsets, L);
         if (np <= kGiantMin) continue;
         const uint32_t ns = (np + kGiantSlice - 1) / kGiantSlice;
@@ -711,9 +721,10 @@ __global__ void __launch_bounds__(kHotThreads) k_fixup_giant_join(const uint2* _
                                                                   xyzz* __restrict__ tail)
 {
     __shared__ xyzz sh[kHotThreads / 32];
-    const uint32_t nh = *hot_count;
-    for (uint32_t h = blockIdx.x; h < nh; h += gridDim.x) {
-        const uint2 e = hot_list[h];
+    const uint2* giants = hot_list + hot_count[0];
+    const uint32_t ng = hot_count[2];
+    for (uint32_t h = blockIdx.x; h < ng; h += gridDim.x) {
+        const uint2 e = giants[h];
         const uint32_t np = hot_parts<Seg>(e.x, e.y, offsets, L);
         if (np <= kGiantMin) continue;
         const uint32_t ns = (np + kGiantSlice - 1) / kGiantSlice;
@@ -1125,7 +1136,7 @@ static cudaError_t msm_run(Ctx* ctx, const void* d_points, const uint8_t* d_scal
 
     CATMSM_CHECK(cudaMemsetAsync(counts, 0, M * 4, st));
     CATMSM_CHECK(cudaMemsetAsync(buckets, 0, M * sizeof(xyzz), st));
-    CATMSM_CHECK(cudaMemsetAsync(hot_count, 0, 8, st));   // hot list and rest list counts
+    CATMSM_CHECK(cudaMemsetAsync(hot_count, 0, 12, st));  // hot, rest and giant list counts
     mark(1);
     if (tile_window)
         k_tile_digits<<<div_up(n, 256), 256, 0, st>>>(d_scalars, stride, (uint32_t)n, nbits, tile_bit0, tile_window, c,

@@ -56,7 +56,7 @@ __global__ void k_fixup(const uint32_t* __restrict__ sorted_key, const uint32_t*
 __global__ void k_fixup_rest(const uint2* __restrict__ hot_list, const uint32_t* __restrict__ hot_count,
                              uint32_t cap, const uint32_t* __restrict__ offsets, uint32_t L,
                              xyzz* __restrict__ buckets, const xyzz* __restrict__ head);
-__global__ void k_fixup_hot(const uint2* __restrict__ hot_list, const uint32_t* __restrict__ hot_count,
+__global__ void k_fixup_hot(uint2* __restrict__ hot_list, uint32_t* __restrict__ hot_count,
                             const uint32_t* __restrict__ offsets, uint32_t L, xyzz* __restrict__ buckets,
                             const xyzz* __restrict__ head, const xyzz* __restrict__ tail);
 __global__ void k_reduce_level(const xyzz* __restrict__ inA, const xyzz* __restrict__ inQ, uint32_t m_in,
@@ -158,7 +158,7 @@ static cudaError_t noalloc_run(const blst_p1_affine* points, const blst_byte* sc
     // regions read before they are written in this call start at zero
     CATMSM_CHECK(cudaMemsetAsync(counts, 0, M * 4, st));
     CATMSM_CHECK(cudaMemsetAsync(buckets, 0, M * sizeof(xyzz), st));
-    CATMSM_CHECK(cudaMemsetAsync(hot_count, 0, 8, st));
+    CATMSM_CHECK(cudaMemsetAsync(hot_count, 0, 12, st));
     k_digits<<<div_up(n, 256), 256, 0, st>>>(d_sc, nbytes, (uint32_t)n, nbits, kC, D, digits, ranks, counts);
     k_scan_local<<<nblocks, 1024, 0, st>>>(counts, offsets, bsums, (uint32_t)M);
     k_scan_top<<<1, 1024, 0, st>>>(bsums, nblocks, total);
