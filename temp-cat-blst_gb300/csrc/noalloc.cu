@@ -74,6 +74,10 @@ constexpr size_t kM = (size_t)kMaxD * kB;
 constexpr size_t kND = kMaxPoints * kMaxD;
 constexpr uint32_t kL = 16;
 constexpr size_t kChunks = (kND + kL - 1) / kL;
+// A bucket holds at most kMaxPoints entries, so its carries span at most
+// kMaxPoints / kL + 1 chunks: within k_fixup_hot's block join (1024
+// partials), and the grid-wide joins of the regular pipeline are not needed.
+static_assert(kMaxPoints / kL + 1 <= 1024, "noalloc buckets must stay within the block join");
 constexpr size_t kLvl1 = (size_t)kMaxD * (kB / 8);
 constexpr size_t kLvl2 = (size_t)kMaxD * (kB / 16) + kMaxD;
 constexpr int kScanTileNa = 1024 * 4;   // k_scan_local's tile (1024 threads x 4)
