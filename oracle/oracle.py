@@ -335,6 +335,9 @@ class Reference(_Common):
         L.blst_p1_fft_with_domain.argtypes = [_vp, _sz, _vp, _sz, C.c_bool]
         L.blst_p1_ifft_unscaled_with_domain.restype = C.c_bool
         L.blst_p1_ifft_unscaled_with_domain.argtypes = [_vp, _sz, _vp, _sz]
+        if hasattr(L, "refshim_p1_fft_truncated_prefix"):
+            L.refshim_p1_fft_truncated_prefix.restype = C.c_bool
+            L.refshim_p1_fft_truncated_prefix.argtypes = [_vp, _sz, _sz, _vp]
         L.blst_fr_fft.restype = C.c_bool
         L.blst_fr_fft.argtypes = [_vp, _sz, C.c_bool]
         L.blst_fr_fft_with_domain.restype = C.c_bool
@@ -412,6 +415,14 @@ class Reference(_Common):
     def p1_ifft_unscaled_with_domain(self, values, n, domain, domain_len):
         b = bytearray(values)
         ok = self.L.blst_p1_ifft_unscaled_with_domain(_buf(b), n, _buf(domain), domain_len)
+        return ok, bytes(b)
+
+    def p1_fft_truncated_prefix(self, values, n, xn, domain, domain_len):
+        """The reference's fft_forward_truncated_prefix template (through
+        oracle/ref_shim.cpp) over the domain's first n roots."""
+        assert domain_len == n + 2 and 0 < xn <= n
+        b = bytearray(values)
+        ok = self.L.refshim_p1_fft_truncated_prefix(_buf(b), n, xn, _buf(domain))
         return ok, bytes(b)
 
     def fr_fft(self, values, n, inverse):

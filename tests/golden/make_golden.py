@@ -20,7 +20,11 @@ reference's own C ABI built from its sources (oracle/_ref/libblst_ref.so):
 
   * tile:   blst_p1s_tile_pippenger -> compressed, per (n, nbits, bit0, window)
 
-`--section wbits|msm_fr_variants|tile` regenerates only that section of an
+  * fft_truncated: the reference's fft_forward_truncated_prefix template (C
+            entry in oracle/ref_shim.cpp) -> sha256 of blst_p1_serialize of
+            every element, per (seed, n, xn); each equals the full transform
+
+`--section wbits|msm_fr_variants|tile|fft_truncated` regenerates only that section of an
 existing file.
 """
 import hashlib
@@ -134,6 +138,29 @@ def tile_section(o, r):
     return out
 
 
+def fft_truncated_section(o, r):
+    """Truncated-prefix forward G1 FFT (the reference's C++ template through
+    oracle/ref_shim.cpp): seeded Jacobian inputs with [xn, n) the identity,
+    the domain's roots.  Each case also checks the reference's own property
+    that the output equals its full forward transform."""
+    out = []
+    for seed, n, xns in ((41, 32, (1, 5, 13, 24, 32)), (42, 1024, (1, 2, 3, 100, 511, 512, 513, 1000, 1024)),
+                         (43, 4096, (1, 7, 1024, 2049, 4096))):
+        d = r.domain(n)
+        base = o.jacobian_randomize(seed, n, o.gen_points(seed, n))
+        for xn in xns:
+            t = time.time()
+            jac = base[:144 * xn] + bytes(144 * (n - xn))
+            ok, tr = r.p1_fft_truncated_prefix(jac, n, xn, d, n + 2)
+            ok2, full = r.p1_fft_with_domain(jac, n, d, n + 2, False)
+            assert ok and ok2
+            ser = b"".join(r.serialize(tr[144 * i:144 * i + 144]) for i in range(n))
+            assert ser == b"".join(r.serialize(full[144 * i:144 * i + 144]) for i in range(n))
+            out.append({"seed": seed, "n": n, "xn": xn, "sha256": hashlib.sha256(ser).hexdigest()})
+            print("fft_truncated", seed, n, xn, "%.1fs" % (time.time() - t), flush=True)
+    return out
+
+
 def main():
     large = "--large" in sys.argv
     build(ref=True)
@@ -141,7 +168,8 @@ def main():
     if "--section" in sys.argv:
         name = sys.argv[sys.argv.index("--section") + 1]
         g = json.load(open(OUT))
-        g[name] = {"wbits": wbits_section, "msm_fr_variants": fr_variants_section, "tile": tile_section}[name](o, r)
+        g[name] = {"wbits": wbits_section, "msm_fr_variants": fr_variants_section, "tile": tile_section,
+                   "fft_truncated": fft_truncated_section}[name](o, r)
         json.dump(g, open(OUT, "w"), indent=1)
         print("wrote", OUT)
         return
@@ -224,6 +252,7 @@ def main():
     g["wbits"] = wbits_section(o, r)
     g["msm_fr_variants"] = fr_variants_section(o, r)
     g["tile"] = tile_section(o, r)
+    g["fft_truncated"] = fft_truncated_section(o, r)
     if not large and os.path.exists(OUT):
         # keep previously generated large cases
         old = json.load(open(OUT))

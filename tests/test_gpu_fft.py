@@ -180,6 +180,23 @@ def _padded(oracle, seed, n, xn):
     return bytes(jac)
 
 
+def test_fft_truncated_prefix_matches_golden(gpu, oracle, golden):
+    """catmsm_p1_fft_truncated_prefix against the reference template's own
+    outputs (golden fft_truncated: n = 32, 1024, 4096, xn from 1 to n)."""
+    cases = golden["fft_truncated"]
+    assert len(cases) >= 19
+    base = {}
+    for c in cases:
+        n, xn = c["n"], c["xn"]
+        if (c["seed"], n) not in base:
+            base[(c["seed"], n)] = oracle.jacobian_randomize(c["seed"], n, oracle.gen_points(c["seed"], n))
+        jac = base[(c["seed"], n)][:144 * xn] + bytes(144 * (n - xn))
+        ok, tr = gpu.p1_fft_truncated_prefix(jac, n, xn, gpu.fr_fft_domain_init(n)[1], n + 2)
+        assert ok
+        ser = b"".join(oracle.serialize(tr[144 * i:144 * i + 144]) for i in range(n))
+        assert hashlib.sha256(ser).hexdigest() == c["sha256"], (n, xn)
+
+
 def test_fft_truncated_prefix_matches_oracle(gpu, oracle):
     """catmsm_p1_fft_truncated_prefix against the oracle's restatement of the
     reference's truncated-prefix plan (and so against the full transform),

@@ -287,3 +287,21 @@ def test_oracle_fft_truncated_prefix_matches_full(oracle):
     assert not oracle.p1_fft_truncated_prefix(zero, m, m + 1, d, m + 2)[0]
     assert not oracle.p1_fft_truncated_prefix(zero, m, 4, d, m + 1)[0]
 
+
+def test_oracle_fft_truncated_prefix_matches_golden(golden, oracle):
+    """The oracle's restatement of the truncated-prefix plan against the
+    reference template's outputs (golden fft_truncated, n <= 1024 here; the
+    GPU test covers every case)."""
+    cases = [c for c in golden["fft_truncated"] if c["n"] <= 1024]
+    assert len(cases) >= 14
+    base = {}
+    for c in cases:
+        n, xn = c["n"], c["xn"]
+        if (c["seed"], n) not in base:
+            base[(c["seed"], n)] = oracle.jacobian_randomize(c["seed"], n, oracle.gen_points(c["seed"], n))
+        jac = base[(c["seed"], n)][:144 * xn] + bytes(144 * (n - xn))
+        ok, tr = oracle.p1_fft_truncated_prefix(jac, n, xn, oracle.domain(n), n + 2)
+        assert ok
+        ser = b"".join(oracle.serialize(tr[144 * i:144 * i + 144]) for i in range(n))
+        assert hashlib.sha256(ser).hexdigest() == c["sha256"], (n, xn)
+
