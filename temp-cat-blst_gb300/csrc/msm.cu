@@ -869,6 +869,7 @@ __global__ void __launch_bounds__(128) k_reduce_pair(const xyzz* __restrict__ in
 // first level so that many windows fit on an SM.
 constexpr int kTailThreads = 256;
 constexpr size_t kFanIn8MinBuckets = size_t(1) << 18;   // all windows' buckets
+constexpr size_t kFanIn16MinBuckets = size_t(1) << 20;
 constexpr uint32_t kQuadMaxNodes = 8192;                  // a level of at most this many nodes uses quads
 
 __global__ void __launch_bounds__(kTailThreads) k_reduce_tail(const xyzz* __restrict__ inA,
@@ -1107,9 +1108,11 @@ static cudaError_t msm_run(Ctx* ctx, const void* d_points, const uint8_t* d_scal
     const size_t chunks = (nD + L - 1) / L;
     // Level 1 of the reduction: fan-in 8 (about 2.4 additions per bucket, but
     // a 19-operation dependent chain) when there are enough buckets to keep
-    // every SM busy; otherwise fan-in 2 with the pair kernel straight from the
-    // buckets (Q = B_0 + 2 B_1, A = 2 (B_0 + B_1): two operations per level).
-    const uint32_t S = M >= kFanIn8MinBuckets ? 8 : 2;
+    // every SM busy, fan-in 16 (about 2.1 per bucket and half the nodes for
+    // the levels above; a 34-operation chain) when there are many more;
+    // otherwise fan-in 2 with the pair kernel straight from the buckets
+    // (Q = B_0 + 2 B_1, A = 2 (B_0 + B_1): two operations per level).
+    const uint32_t S = M >= kFanIn16MinBuckets ? 16 : M >= kFanIn8MinBuckets ? 8 : 2;
     const size_t lvl1 = (size_t)D * ((B + S - 1) / S);
     const size_t lvl2 = (size_t)D * ((B + 2 * S - 1) / (2 * S)) + D;
 
@@ -1186,7 +1189,7 @@ static cudaError_t msm_run(Ctx* ctx, const void* d_points, const uint8_t* d_scal
         const xyzz* inA = buckets;
         const xyzz* inQ = S == 2 ? buckets : nullptr;
         uint32_t m = B, pp = 0;
-        bool first = S == 8;
+        bool first = S != 2;
         while (m > 1) {
             if (!first && m <= msm_reduce_tail_max(D)) {
                 msm_reduce_tail(inA, inQ, m, D, bufQ[pp], st);
@@ -1198,8 +1201,8 @@ static cudaError_t msm_run(Ctx* ctx, const void* d_points, const uint8_t* d_scal
             const uint32_t F = first ? S : 2;
             const uint32_t m_out = (m + F - 1) / F;
             if (first)
-                k_reduce_level<<<div_up((size_t)D * m_out, 128), 128, 0, st>>>(inA, inQ, m, F, 3, D, 1, bufA[pp],
-                                                                              bufQ[pp]);
+                k_reduce_level<<<div_up((size_t)D * m_out, 128), 128, 0, st>>>(inA, inQ, m, F, S == 16 ? 4 : 3, D, 1,
+                                                                              bufA[pp], bufQ[pp]);
             else
                 msm_reduce_pair(inA, inQ, m, D, bufA[pp], bufQ[pp], st);
             g_stats.launches++;
