@@ -283,7 +283,7 @@ def _jac_affine(p144: bytes):
 
 
 def batched_section(g, synth, torch, dev, steps, warmup, peak):
-    """BASELINE config 3: 1024 commitments per batch over a resident 4096-point
+    """Batched commitments: 1024 commitments per batch over a resident 4096-point
     basis, k_j = floor(2^U), U ~ U[8, 12] (seeded), uniform Fr scalars; the
     batch runs as one CUDA-graph launch with the autotuned (window, chunk);
     compared with the same 1024 MSMs through the plain per-call device path."""
@@ -354,7 +354,7 @@ def _jacobian_z1(aff: bytes, n: int) -> bytes:
 
 
 def batched_fft_section(g, synth, torch, dev, steps, warmup, peak):
-    """BASELINE config 4: 64 transforms per batch, 16 each of 2^10, 2^12, 2^14,
+    """Batched G1 FFT: 64 transforms per batch, 16 each of 2^10, 2^12, 2^14,
     2^16 in a seeded order, seeded points in Jacobian form, prepared domains;
     forward and inverse batches through catmsm_p1_fft_batch (host buffers, one
     launch per stage level for all transforms) vs the same 64 transforms as
@@ -468,7 +468,7 @@ def decode_section(g, synth, torch, dev, steps, warmup):
 
 
 def serving_section(g, synth, torch, dev, rates, seconds):
-    """BASELINE config 5: Poisson arrivals (swept rate) of 70% MSMs with k
+    """Serving: Poisson arrivals (swept rate) of 70% MSMs with k
     log-uniform in [2^10, 2^22] over a resident 2^22-point basis (fixed-base
     tables) and 30% G1 FFTs with n = 2^(12..16); served by the continuous-
     batching engine vs a plain FIFO server making one per-call request at a

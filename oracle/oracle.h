@@ -3,7 +3,7 @@
  *
  * TEST INFRASTRUCTURE ONLY.  This is a plain C11 restatement of the reference
  * library's algorithms (category-blst), used by tests/, the smoke check and
- * bench.py's CPU-baseline leg as the checker.  The product library never
+ * bench.py's CPU-baseline leg to check results.  The product library never
  * links, loads or calls anything declared here.
  *
  * Parity of this restatement is pinned against the reference library built

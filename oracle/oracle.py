@@ -1,4 +1,4 @@
-"""ctypes access to the CPU checkers (test infrastructure only).
+"""ctypes access to the CPU oracle libraries (test infrastructure only).
 
 * ``Oracle``     -- the C restatement in this directory (liboracle.so).
 * ``Reference``  -- the reference library compiled from its own sources
