@@ -236,6 +236,15 @@ size_t catmsm_msm_window(size_t npoints);
  * split enabled).  Returns 0, or -1 on invalid arguments. */
 int catmsm_msm_plan(size_t npoints, size_t nbits, size_t *window, size_t *windows, size_t *points);
 
+/* The same plan without a context (host arithmetic only, no GPU needed):
+ * glv = 1 applies the GLV split as the library does by default.  Also
+ * reports the bucket-accumulation chunk length (entries per thread) and the
+ * reduction's level-1 fan-in (2, 8 or 16).  Off a GPU the chunk model uses
+ * the GB300's 152 SMs x 4 resident blocks.  Returns 0, or -1 on invalid
+ * arguments. */
+int catmsm_msm_plan_detail(size_t npoints, size_t nbits, int glv, size_t *window, size_t *windows, size_t *points,
+                           size_t *chunk, size_t *fan_in);
+
 /* Enables (1) or disables (0) the GLV split for the calling thread's MSMs
  * (on by default; -1 only queries).  Returns the previous setting, or -1
  * without a device context.  Both settings give the same group element for

@@ -87,6 +87,8 @@ def load(build_if_missing=True):
     L.catmsm_msm_window.argtypes = [_sz]
     L.catmsm_msm_plan.restype = C.c_int
     L.catmsm_msm_plan.argtypes = [_sz, _sz, _vp, _vp, _vp]
+    L.catmsm_msm_plan_detail.restype = C.c_int
+    L.catmsm_msm_plan_detail.argtypes = [_sz, _sz, C.c_int, _vp, _vp, _vp, _vp, _vp]
     L.catmsm_msm_glv.restype = C.c_int
     L.catmsm_msm_glv.argtypes = [C.c_int]
     L.catmsm_p1_affines_from_scalars.restype = C.c_int
@@ -446,6 +448,14 @@ def msm_plan(n: int, nbits: int = 255):
     c, d, p = _sz(), _sz(), _sz()
     assert load().catmsm_msm_plan(n, nbits, C.byref(c), C.byref(d), C.byref(p)) == 0
     return c.value, d.value, p.value
+
+
+def msm_plan_detail(n: int, nbits: int = 255, glv: int = 1):
+    """(window, windows, pipeline points, chunk length, level-1 fan-in) of an
+    MSM; host arithmetic only, no GPU needed."""
+    v = [_sz() for _ in range(5)]
+    assert load().catmsm_msm_plan_detail(n, nbits, glv, *[C.byref(x) for x in v]) == 0
+    return tuple(x.value for x in v)
 
 
 def msm_glv(enable: int = -1) -> int:

@@ -439,6 +439,21 @@ int catmsm_msm_glv(int enable)
     return prev;
 }
 
+int catmsm_msm_plan_detail(size_t npoints, size_t nbits, int glv, size_t* window, size_t* windows, size_t* points,
+                           size_t* chunk, size_t* fan_in)
+{
+    if (npoints == 0 || nbits == 0 || nbits > 256 || !window || !windows || !points || !chunk || !fan_in) return -1;
+    uint32_t c, D, L, S;
+    size_t np;
+    msm_plan_detail(npoints, (uint32_t)nbits, glv != 0, &c, &D, &np, &L, &S);
+    *window = c;
+    *windows = D;
+    *points = np;
+    *chunk = L;
+    *fan_in = S;
+    return 0;
+}
+
 int catmsm_msm_plan(size_t npoints, size_t nbits, size_t* window, size_t* windows, size_t* points)
 {
     Ctx* ctx = get_ctx();

@@ -23,6 +23,8 @@ int basis_device(const Basis* b);
 // Window width, window count and pipeline point count msm_device uses for
 // n points of nbits-bit scalars on this context (2n points of 127 bits when
 // the GLV split applies).
+void msm_plan_detail(size_t n, uint32_t nbits, bool glv, uint32_t* c, uint32_t* windows, size_t* points,
+                     uint32_t* chunk, uint32_t* fan_in);
 void msm_plan(const Ctx* ctx, size_t n, uint32_t nbits, uint32_t* c, uint32_t* windows, size_t* points);
 
 // Per-device set-up of the MSM kernels (shared-memory limits), run once per

@@ -1040,6 +1040,26 @@ static bool use_glv(const Ctx* ctx, size_t n, uint32_t nbits)
     return ctx->glv && nbits > 128 && n < (1u << 30);
 }
 
+static uint32_t level1_fan_in(size_t M)
+{
+    return M >= kFanIn16MinBuckets ? 16 : M >= kFanIn8MinBuckets ? 8 : 2;
+}
+
+// The plan without a context (host arithmetic only; off a GPU the chunk
+// model uses 152 SMs x 4 resident blocks, the GB300's figures): window,
+// windows, pipeline points, accumulate chunk length and level-1 fan-in.
+void msm_plan_detail(size_t n, uint32_t nbits, bool glv, uint32_t* c, uint32_t* windows, size_t* points,
+                     uint32_t* chunk, uint32_t* fan_in)
+{
+    const bool g = glv && nbits > 128 && n < (1u << 30);
+    const size_t np = g ? 2 * n : n;
+    *c = g ? msm_glv_window(np) : msm_default_window(np);
+    *windows = (g ? 127 : nbits) / *c + 1;
+    *points = np;
+    *chunk = accumulate_chunk(np * *windows);
+    *fan_in = level1_fan_in((size_t)*windows << (*c - 1));
+}
+
 void msm_plan(const Ctx* ctx, size_t n, uint32_t nbits, uint32_t* c, uint32_t* windows, size_t* points)
 {
     const bool g = use_glv(ctx, n, nbits);
@@ -1112,7 +1132,7 @@ static cudaError_t msm_run(Ctx* ctx, const void* d_points, const uint8_t* d_scal
     // the levels above; a 34-operation chain) when there are many more;
     // otherwise fan-in 2 with the pair kernel straight from the buckets
     // (Q = B_0 + 2 B_1, A = 2 (B_0 + B_1): two operations per level).
-    const uint32_t S = M >= kFanIn16MinBuckets ? 16 : M >= kFanIn8MinBuckets ? 8 : 2;
+    const uint32_t S = level1_fan_in(M);
     const size_t lvl1 = (size_t)D * ((B + S - 1) / S);
     const size_t lvl2 = (size_t)D * ((B + 2 * S - 1) / (2 * S)) + D;
 

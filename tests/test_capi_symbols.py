@@ -69,3 +69,28 @@ def test_fr_msm_variant_sizes_match_reference(gpu_binding, golden):
         assert gpu_binding.p1s_mult_fr_scratch_sizeof(n) == exp, n
     for n, w, b, exp in g["batch_affine_scratch"]:
         assert gpu_binding.p1s_mult_batch_affine_fr_scratch_sizeof(n, w, b) == exp, (n, w, b)
+
+
+def test_msm_plan_heuristics(gpu_binding):
+    """Host arithmetic only: the window model, the bucket-accumulation chunk
+    length (partial-wave model below ~one wave, whole waves above) and the
+    reduction's level-1 fan-in, pinned at the sizes they were measured and
+    tuned at on a GB300 (152 SMs x 4 resident blocks).  A change here changes
+    the GPU schedule and must be re-measured."""
+    # n: (window, windows, pipeline points, chunk, level-1 fan-in), GLV on
+    expected = {
+        1 << 10: (8, 16, 1 << 11, 4, 2),
+        1 << 12: (10, 13, 1 << 13, 6, 2),
+        1 << 14: (11, 12, 1 << 15, 11, 2),
+        1 << 16: (13, 10, 1 << 17, 34, 2),
+        1 << 17: (13, 10, 1 << 18, 45, 2),
+        1 << 18: (16, 8, 1 << 19, 54, 8),
+        1 << 20: (16, 8, 1 << 21, 72, 8),
+        1 << 22: (19, 7, 1 << 23, 84, 16),
+    }
+    for n, exp in expected.items():
+        assert gpu_binding.msm_plan_detail(n) == exp, n
+    # no GLV split: 255-bit windows over n points; 64-bit scalars skip the split
+    assert gpu_binding.msm_plan_detail(1 << 20, 255, 0)[:3] == (16, 16, 1 << 20)
+    assert gpu_binding.msm_plan_detail(1 << 16, 64)[:3] == (12, 6, 1 << 16)
+
