@@ -94,3 +94,20 @@ def test_msm_plan_heuristics(gpu_binding):
     assert gpu_binding.msm_plan_detail(1 << 20, 255, 0)[:3] == (16, 16, 1 << 20)
     assert gpu_binding.msm_plan_detail(1 << 16, 64)[:3] == (12, 6, 1 << 16)
 
+
+def test_fft_truncated_prefix_rejects_on_the_host(gpu_binding, oracle):
+    """catmsm_p1_fft_truncated_prefix checks its arguments on the host before
+    any device work: a bad size, domain length or tag, xn = 0 or xn > n, or a
+    non-identity element past xn returns false with the values untouched."""
+    n = 16
+    d = oracle.domain(n)
+    jac = bytearray(oracle.jacobian_randomize(7, n, oracle.gen_points(7, n)))
+    jac[144 * 6:] = bytes(144 * (n - 6))
+    jac = bytes(jac)
+    bad_tag = bytearray(d)
+    bad_tag[-32] ^= 1
+    for args in ((jac, n, 0, d, n + 2), (jac, n, n + 1, d, n + 2), (jac, n, 6, d, n + 1),
+                 (jac, n, 6, bytes(bad_tag), n + 2), (jac, 12, 6, d, 14), (jac, n, 5, d, n + 2)):
+        ok, out = gpu_binding.p1_fft_truncated_prefix(*args)
+        assert not ok and out == jac
+
