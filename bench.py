@@ -39,6 +39,7 @@ SEED = 6                  # points: P_i = k_i G, k_i = synth.point_scalars(6); s
 GOLDEN_2_20 = "90cd36b5979df69caa70eb7aac8aef471ca3fb41af29c0d6fc1dd5e13532cd7ce5b294e10e96084057b494f1009a2729"
 IMAD_PER_M = 576
 MADD_M = 10               # XYZZ mixed add, 8M + 2S
+ACC_BYTES_PER_ENTRY = 96 + 8   # bucket accumulation reads per entry: the affine point, its index and key
 
 
 def _load(name, path):
@@ -197,39 +198,25 @@ def traffic_from_profile():
     return None
 
 
-def cpu_tile_sample(o, pts, sc, n, threads, budget_s=12.0):
-    """Reference-algorithm CPU throughput from whole single-window tiles of
-    the same 2^20 workload (window c = 17 as the reference picks for 2^20;
-    a full MSM is D = 16 such tiles plus a negligible fold).  Returns
-    (Mpoints/s, tiles, seconds)."""
-    c = ref_window(n)
-    D = 1 + NBITS // c
-    mids = list(range(1, D - 1))
-    done = [0]
-    lock = threading.Lock()
-    t0 = time.perf_counter()
-
-    def work(tid):
-        k = 0
-        while True:
-            with lock:
-                if time.perf_counter() - t0 > budget_s and done[0] >= threads:
-                    return
-                done[0] += 1
-            o.tile_seconds(pts, sc, n, NBITS, c * mids[(tid + k * threads) % len(mids)], c, 1)
-            k += 1
-
-    ths = [threading.Thread(target=work, args=(i,)) for i in range(threads)]
-    for t in ths:
-        t.start()
-    for t in ths:
-        t.join()
-    el = time.perf_counter() - t0
-    tiles = done[0]
-    return (tiles / D) * n / el / 1e6, tiles, el
+def executed_imad_from_profile():
+    """Executed fmaheavy-pipe (IMAD) thread instructions per batched-
+    commitments batch, from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "batched_commitments_imad.txt")
+    try:
+        for line in open(path):
+            if line.startswith("imad_thread_inst_per_batch:"):
+                return float(line.split(":", 1)[1].split()[0])
+    except OSError:
+        pass
+    return None
 
 
 def run_reference(args, ws, rank):
+    """The reference algorithm on the host cores: whole MSM calls of the
+    measured workload (the C restatement of the reference's Pippenger,
+    oracle/, since the reference tree is not on the GPU host), one call per
+    step, the steps spread over every host thread; value = points of all
+    timed calls / wall time of the timed calls."""
     if rank != 0:
         return 0
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -241,26 +228,33 @@ def run_reference(args, ws, rank):
     threads = os.cpu_count() or 1
     pts = o.points_from_scalars(synth.point_scalars(SEED, n), n, threads)
     sc = synth.scalars(SEED + 1000, n, 0)
-    c = ref_window(n)
-    D = 1 + NBITS // c
-    for _ in range(args.warmup):
-        cpu_tile_sample(o, pts, sc, n, threads, budget_s=0.0)
-    vals = []
-    for _ in range(args.steps):
-        v, tiles, el = cpu_tile_sample(o, pts, sc, n, threads, budget_s=0.0)
-        vals.append((v, el))
-    value = statistics.mean(v for v, _ in vals)
-    ms = statistics.mean(e for _, e in vals) * 1e3
+
+    def run_calls(count):
+        """count whole calls over min(threads, count) threads; (wall s, per-call s, results)."""
+        import concurrent.futures as cf
+        t0 = time.perf_counter()
+        with cf.ThreadPoolExecutor(max_workers=max(1, min(threads, count))) as ex:
+            res = list(ex.map(lambda _: o.msm_seconds(pts, sc, n, NBITS), range(count)))
+        return time.perf_counter() - t0, [r[0] for r in res], [r[1] for r in res]
+
+    if args.warmup:
+        run_calls(min(args.warmup, threads))
+    wall, per_call, outs = run_calls(args.steps)
+    value = args.steps * n / wall / 1e6
+    parity = all(r.hex() == GOLDEN_2_20 for r in outs) if n == N_POINTS else None
+    used = max(1, min(threads, args.steps))
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic (seeded)",
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": statistics.mean(per_call) * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+        "data": "synthetic (seeded)",
         "config": {"workload": "G1 MSM n=2^20, uniform 255-bit Fr scalars", "n": n, "nbits": NBITS},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": "each step: %d threads each run one whole single-window tile "
-                                   "(c=%d, 1 of D=%d windows) of the same 2^%d-point MSM with the "
-                                   "reference's Pippenger restated in C (oracle/); Mpoints/s = "
-                                   "tiles/D * n / step time" % (threads, c, D, n.bit_length() - 1)},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": used, "kind": "port",
+                         "sample": "%d whole 2^%d-point MSM calls (one per step, window c=%d as the reference "
+                                   "picks) of the reference's Pippenger restated in C (oracle/), spread over %d "
+                                   "host threads; %.1f s wall; ms_per_step = mean single-call time"
+                                   % (args.steps, n.bit_length() - 1, ref_window(n), used, wall)},
+        "parity_vs_reference_golden": parity,
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -280,6 +274,64 @@ def _jac_affine(p144: bytes):
     y = int.from_bytes(p144[48:96], "little") * rinv % P_MOD
     zi = pow(z, -1, P_MOD)
     return x * zi * zi % P_MOD, y * zi * zi * zi % P_MOD
+
+
+def _affine_many(blobs):
+    """Affine (x, y) integers of many Jacobian blst_p1 (Montgomery form), None
+    for infinity, with one modular inversion for all of them (Montgomery's
+    trick over the nonzero z)."""
+    rinv = pow(1 << 384, -1, P_MOD)
+    zs = [int.from_bytes(b[96:144], "little") * rinv % P_MOD for b in blobs]
+    prefix, acc = [], 1
+    for z in zs:
+        prefix.append(acc)
+        if z:
+            acc = acc * z % P_MOD
+    inv = pow(acc, -1, P_MOD)
+    out = [None] * len(zs)
+    for i in range(len(zs) - 1, -1, -1):
+        z = zs[i]
+        if not z:
+            continue
+        zi = inv * prefix[i] % P_MOD
+        inv = inv * z % P_MOD
+        zi2 = zi * zi % P_MOD
+        x = int.from_bytes(blobs[i][0:48], "little") * rinv % P_MOD
+        y = int.from_bytes(blobs[i][48:96], "little") * rinv % P_MOD
+        out[i] = (x * zi2 % P_MOD, y * zi2 * zi % P_MOD)
+    return out
+
+
+def _compress_xy(xy) -> bytes:
+    """blst_p1_compress encoding of an affine point (None = infinity)."""
+    if xy is None:
+        return bytes([0xC0]) + bytes(47)
+    out = bytearray(xy[0].to_bytes(48, "big"))
+    out[0] |= 0x80 | (0x20 if xy[1] > (P_MOD - 1) // 2 else 0)
+    return bytes(out)
+
+
+def _serialize_xy(xy) -> bytes:
+    """blst_p1_serialize encoding of an affine point (None = infinity)."""
+    if xy is None:
+        return bytes([0x40]) + bytes(95)
+    return xy[0].to_bytes(48, "big") + xy[1].to_bytes(48, "big")
+
+
+def _split144(buf: bytes, count: int):
+    return [buf[144 * j:144 * j + 144] for j in range(count)]
+
+
+_GOLDEN = None
+
+
+def golden():
+    """The reference's golden outputs (tests/golden/golden.json)."""
+    global _GOLDEN
+    if _GOLDEN is None:
+        with open(os.path.join(ROOT, "tests", "golden", "golden.json")) as f:
+            _GOLDEN = json.load(f)
+    return _GOLDEN
 
 
 def batched_section(g, synth, torch, dev, steps, warmup, peak):
@@ -327,7 +379,13 @@ def batched_section(g, synth, torch, dev, steps, warmup, peak):
         el = time.perf_counter() - t
     t_plain = el
     parity = all(_jac_affine(out[144 * j:144 * j + 144]) == _jac_affine(plain[j]) for j in range(16))
+    gb = golden().get("batch_commitments")
+    gold_ok = None
+    if gb and gb["counts"] == counts:
+        got = [_compress_xy(xy).hex() for xy in _affine_many(_split144(out, nmsm))]
+        gold_ok = got == gb["compressed"]
     cm = sum(canonical_m(k, 255) for k in counts)
+    executed = executed_imad_from_profile()
     b.close()
     return {"workload": "1024 MSMs/batch, k log-uniform in [256, 4096] over a resident 4096-point basis "
                         "with fixed-base tables, uniform Fr scalars",
@@ -337,8 +395,138 @@ def batched_section(g, synth, torch, dev, steps, warmup, peak):
             "canonical_timad_s": cm * IMAD_PER_M / t_batch / 1e12,
             "canonical_frac_of_peak": cm * IMAD_PER_M / t_batch / 1e12 / peak if peak > 0 else None,
             "parity_vs_plain_path_first16": parity,
+            "parity_vs_reference_golden_all": gold_ok,
+            "executed": ({"imad_per_batch": executed, "fp_mul_equiv_per_batch": executed / IMAD_PER_M,
+                          "timad_s": executed / t_batch / 1e12,
+                          "frac_of_peak": executed / t_batch / 1e12 / peak if peak > 0 else None,
+                          "source": "ncu sm__thread_inst_executed_pipe_fmaheavy_pred_on.sum over the batch's "
+                                    "kernels (profiles/batched_commitments_imad.txt)"} if executed else None),
             "timing": "host wall clock around each synchronous batch call (H2D of the scalars from pinned "
                       "host memory, one graph launch, D2H of results)"}
+
+
+def _device_points(g, synth, torch, dev, seed, n):
+    """The seeded point set P_i = k_i G (k = synth.point_scalars(seed, n)) on
+    the device, generated by the library's fixed-base comb kernel."""
+    k_pts = torch.frombuffer(bytearray(synth.point_scalars(seed, n)), dtype=torch.uint8).to(dev)
+    d_pts = torch.empty(n * 96, dtype=torch.uint8, device=dev)
+    torch.cuda.synchronize()
+    assert g.load().catmsm_p1_affines_from_scalars_device(d_pts.data_ptr(), k_pts.data_ptr(), n) == 0
+    torch.cuda.synchronize()
+    return d_pts
+
+
+def _time_device_msm(g, torch, stream, flush, fn, steps, warmup):
+    """Mean CUDA-event time (ms) of fn() on the library stream, L2 flushed
+    before every call."""
+    for _ in range(warmup):
+        flush.zero_()
+        torch.cuda.synchronize()
+        fn()
+    ts = []
+    for _ in range(steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        fn()
+        b.record(stream)
+        b.synchronize()
+        ts.append(a.elapsed_time(b))
+    return statistics.mean(ts)
+
+
+def plain_small_section(g, synth, torch, dev, stream, flush, steps, warmup, cpu):
+    """The plain n = 4096 MSM (seed 1, uniform Fr scalars): one
+    blst_p1s_mult_pippenger call from host buffers (H2D, pipeline, result)
+    and the same MSM on device-resident inputs, checked against the
+    reference's golden bytes; beside it the reference algorithm's CPU
+    restatement on the same inputs (1 thread, median of 5 whole calls)."""
+    import ctypes as C
+    import numpy as np
+    n, seed = 4096, 1
+    want = next(c["compressed"] for c in golden()["msm"] if c["seed"] == seed and c["n"] == n)
+    d_pts = _device_points(g, synth, torch, dev, seed, n)
+    sc = synth.scalars(seed + 1000, n, 0)
+    d_sc = torch.frombuffer(bytearray(sc), dtype=torch.uint8).to(dev)
+    h_pts = torch.empty(n * 96, dtype=torch.uint8, pin_memory=True)
+    h_sc = torch.empty(n * 32, dtype=torch.uint8, pin_memory=True)
+    h_pts.copy_(d_pts.cpu())
+    h_sc.numpy()[:] = np.frombuffer(sc, dtype=np.uint8)
+    dev_ms = _time_device_msm(g, torch, stream, flush,
+                              lambda: g.msm_device(d_pts.data_ptr(), d_sc.data_ptr(), 32, n, NBITS), steps, warmup)
+    first = g.msm_device(d_pts.data_ptr(), d_sc.data_ptr(), 32, n, NBITS)
+    L = g.load()
+    parr = (C.c_void_p * 2)(h_pts.data_ptr(), None)
+    sarr = (C.c_void_p * 2)(h_sc.data_ptr(), None)
+    scratch = (C.c_uint64 * (g.scratch_sizeof(n) // 8 + 1))()
+    ret = (C.c_char * 144)()
+    ts = []
+    for i in range(warmup + steps):
+        t = time.perf_counter()
+        L.blst_p1s_mult_pippenger(ret, parr, n, sarr, NBITS, scratch)
+        if i >= warmup:
+            ts.append((time.perf_counter() - t) * 1e3)
+    e2e_ms = statistics.median(ts)
+    res = {"workload": "plain G1 MSM, n=4096 (seed 1), uniform 255-bit Fr scalars, one call",
+           "device_ms": dev_ms, "device_mpoints_s": n / dev_ms / 1e3,
+           "e2e_ms": e2e_ms, "e2e_mpoints_s": n / e2e_ms / 1e3,
+           "e2e_timing": "host wall clock around each synchronous blst_p1s_mult_pippenger call (pinned host "
+                         "buffers, H2D of 512 KB inside), median of %d" % steps,
+           "parity_vs_reference_golden": _compress_hex(first) == want and
+           _compress_hex(bytes(ret)) == want}
+    if cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as om
+        o = om.Oracle()
+        pts = bytes(h_pts.numpy())
+        runs = [o.msm_seconds(pts, sc, n, NBITS) for _ in range(5)]
+        t_cpu = statistics.median(r[0] for r in runs)
+        res["cpu_baseline"] = {"ms": t_cpu * 1e3, "mpoints_s": n / t_cpu / 1e6, "cores": 1, "kind": "port",
+                               "sample": "5 whole calls of the reference's Pippenger restated in C (oracle/), "
+                                         "1 thread, median",
+                               "parity": runs[0][1].hex() == want}
+        res["e2e_speedup_vs_cpu"] = t_cpu * 1e3 / e2e_ms
+    return res
+
+
+LARGE_DISTS = {(0, 255, False): "uniform Fr", (1, 255, False): "64-bit scalars, nbits=255",
+               (1, 64, False): "64-bit scalars packed, nbits=64", (2, 255, True): "10% zeros + 5% duplicated points",
+               (2, 255, False): "10% zeros"}
+
+
+def large_msm_section(g, synth, torch, dev, stream, flush, steps, warmup):
+    """The large single-MSM workload: every golden case at n = 2^16, 2^20 and
+    2^22 (uniform Fr; 64-bit scalars at nbits 255 and packed at nbits 64; 10%
+    zero scalars with 5% duplicated points), device-resident inputs, CUDA-event
+    time per MSM with L2 flushed, and the result against the reference's
+    golden bytes."""
+    rows = []
+    cases = sorted((c for c in golden()["msm"] if c["n"] in (1 << 16, 1 << 20, 1 << 22)),
+                   key=lambda c: (c["n"], c["seed"]))
+    for c in cases:
+        n, nbits = c["n"], c["nbits"]
+        d_pts = _device_points(g, synth, torch, dev, c["seed"], n)
+        if c["dup"]:
+            h = bytearray(d_pts.cpu().numpy().tobytes())
+            synth.apply_duplicates(h, c["seed"], n)
+            d_pts = torch.frombuffer(h, dtype=torch.uint8).to(dev)
+        sc = synth.scalars(c["seed"] + 1000, n, c["kind"])
+        nb = (nbits + 7) // 8
+        if nb != 32:
+            import numpy as np
+            sc = np.frombuffer(sc, dtype=np.uint8).reshape(n, 32)[:, :nb].tobytes()
+        d_sc = torch.frombuffer(bytearray(sc), dtype=torch.uint8).to(dev)
+        torch.cuda.synchronize()
+        fn = lambda: g.msm_device(d_pts.data_ptr(), d_sc.data_ptr(), nb, n, nbits)  # noqa: E731
+        ok = _compress_hex(fn()) == c["compressed"]
+        ms = _time_device_msm(g, torch, stream, flush, fn, steps, warmup)
+        rows.append({"n": n, "seed": c["seed"], "scalars": LARGE_DISTS.get((c["kind"], nbits, c["dup"]), "?"),
+                     "nbits": nbits, "ms": ms, "mpoints_s": n / ms / 1e3, "parity_vs_reference_golden": ok})
+        del d_pts, d_sc
+    return {"workload": "single G1 MSM per call, device-resident inputs, L2 flushed between calls",
+            "rows": rows, "all_parity": all(r["parity_vs_reference_golden"] for r in rows)}
 
 
 def fft_canonical_m(n, inverse=False):
@@ -374,6 +562,7 @@ def batched_fft_section(g, synth, torch, dev, steps, warmup, peak):
     doms = {n: g.fr_fft_domain_init(n)[1] for n in base}
     vals = [base[n] for n in sizes]
     res = {}
+    outs_by_mode = {}
     dlist = [doms[n] for n in sizes]
     for mode, name in ((0, "forward"), (1, "inverse")):
         # timed on caller buffers transformed in place (the C ABI's own
@@ -394,6 +583,7 @@ def batched_fft_section(g, synth, torch, dev, steps, warmup, peak):
         res[name] = {"transforms_per_s": len(sizes) / tb, "ms_per_batch": tb * 1e3,
                      "canonical_timad_s": cm * IMAD_PER_M / tb / 1e12,
                      "canonical_frac_of_peak": cm * IMAD_PER_M / tb / 1e12 / peak if peak > 0 else None}
+        outs_by_mode[mode] = outs
         if mode == 0:
             fwd = outs
     # round trip on one transform of each size, and parity with the per-call path
@@ -415,6 +605,23 @@ def batched_fft_section(g, synth, torch, dev, steps, warmup, peak):
     res["speedup_vs_plain_forward"] = t_plain / (res["forward"]["ms_per_batch"] * 1e-3)
     res["round_trip_ok"] = rt
     res["parity_vs_per_call_path"] = par
+    # every transform of both batches against the reference's output for the
+    # same input (sha256 of each element's serialization)
+    gf = golden().get("bench_fft")
+    gold_ok = None
+    if gf:
+        import hashlib
+        want = {(c["n"], c["mode"]): c["sha256"] for c in gf["cases"]}
+        gold_ok = True
+        for mode, mname in ((0, "dfwd"), (1, "dinv")):
+            seen = {}
+            for i, n in enumerate(sizes):
+                out = outs_by_mode[mode][i]
+                if seen.get(n) != out:      # equal bytes need no second serialization
+                    ser = b"".join(_serialize_xy(xy) for xy in _affine_many(_split144(out, n)))
+                    gold_ok &= hashlib.sha256(ser).hexdigest() == want.get((n, mname))
+                    seen[n] = out
+    res["parity_vs_reference_golden_all"] = gold_ok
     res["workload"] = ("64 transforms/batch: 16 each of 2^10, 2^12, 2^14, 2^16 (seeded order), Jacobian "
                        "inputs (z = 1), prepared domains; host buffers, H2D/D2H inside the timer")
     return res
@@ -721,12 +928,17 @@ def run_ours(args, ws, rank, local):
         import oracle as om
         om.build()
         o = om.Oracle()
-        v, tiles, el = cpu_tile_sample(o, bytes(h_pts.numpy()), sc_host, n, 1, budget_s=12.0)
-        cref = ref_window(n)
-        cpu = {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
-               "sample": "%d whole single-window tiles (c=%d, of D=%d) of the same 2^%d-point MSM, "
-                         "1 thread, %.1f s; the reference's Pippenger restated in C (oracle/)"
-                         % (tiles, cref, 1 + NBITS // cref, n.bit_length() - 1, el)}
+        el, res = o.msm_seconds(bytes(h_pts.numpy()), sc_host, n, NBITS)
+        cpu = {"value": n / el / 1e6, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": "one whole 2^%d-point MSM call (%.1f s), 1 thread: the reference's Pippenger "
+                         "(window c=%d as the reference picks) restated in C (oracle/)"
+                         % (n.bit_length() - 1, el, ref_window(n)),
+               "parity_vs_reference_golden": res.hex() == GOLDEN_2_20 if n == N_POINTS else None}
+    config1 = large = None
+    if ws == 1 and not args.no_configs:
+        config1 = plain_small_section(g, synth, torch, dev, stream, flush, args.steps, args.warmup,
+                                      cpu=not args.no_cpu_baseline)
+        large = large_msm_section(g, synth, torch, dev, stream, flush, max(3, args.steps // 2), args.warmup)
     batched = fft_batch = serving = None
     if ws == 1 and not args.no_batched:
         batched = batched_section(g, synth, torch, dev, args.steps, args.warmup, peak)
@@ -752,12 +964,18 @@ def run_ours(args, ws, rank, local):
                      "traffic": traffic_from_profile(),
                      "peak_source": "measured live: max of mad.lo.u32 (%.2f) and mad.wide.u32 (%.2f, 2 per "
                                     "instruction) independent chains on all SMs" % (peak_lo, peak_wide),
-                     "work": "%.0f bucket entries x %d M x %d IMAD per launch" % (entries, MADD_M, IMAD_PER_M)},
+                     "work": "%.0f bucket entries x %d M x %d IMAD per launch" % (entries, MADD_M, IMAD_PER_M),
+                     "achieved_gbs": entries * ACC_BYTES_PER_ENTRY / (acc_ms * 1e-3) / 1e9,
+                     "achieved_gbs_work": "%d B per bucket entry (the gathered 96-B affine point and the 8 B of "
+                                          "sorted point index and bucket key) / accumulate time"
+                                          % ACC_BYTES_PER_ENTRY},
         "canonical": {"M_msm": cm, "imad": cm * IMAD_PER_M, "achieved_timad_s": canon_tera,
                       "frac_of_peak": canon_tera / peak if peak > 0 else None},
         "stages_ms": {k: v / max(calls, 1) for k, v in stages.items()},
         "parity_vs_reference_golden": parity,
         "cpu_baseline": cpu,
+        "plain_n4096": config1,
+        "large_msm": large,
         "clocks": clk,
         "batched_commitments": batched,
         "batched_fft": fft_batch,
@@ -802,6 +1020,8 @@ def main():
     ap.add_argument("--window", type=int, default=0, help="MSM window width (0 = library default)")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched MSM / FFT sections")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving sweep")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the plain n=4096 and large-MSM (2^16 / 2^20 / 2^22, all distributions) sections")
     ap.add_argument("--only", choices=["batched", "fft", "decode"], default=None,
                     help="run only the batched-commitments, batched-FFT or decoding section (diagnostic line)")
     ap.add_argument("--serve-rates", default="25,50,100,150", help="Poisson arrival rates (requests/s)")

@@ -289,9 +289,12 @@ double catmsm_profile_entries(void);
  * (npoints == 0 or nbits == 0 give infinity), CATMSM_NOALLOC_BAD_ARGUMENT for
  * NULL pointers, or a cudaError_t value.  Runs on the per-thread default
  * stream and returns when the result is in *ret.  All calls share the one
- * scratch array, so calls that overlap on the GPU race: serialise them.  The
- * first call on a device looks up the array's address there; make it before
- * any stream capture. */
+ * scratch array, so calls that overlap on the GPU race: serialise them; a call
+ * that fails after queueing work waits for that work before it returns.  The
+ * first call on a device looks up the array's address there, and with the
+ * CUDA runtime's default lazy module loading that is when the device reserves
+ * the array: make the first call on each device before another framework
+ * claims the GPU's memory and before any stream capture.  Devices 0..63. */
 #define CATMSM_NOALLOC_MAX_POINTS 4096
 #define CATMSM_NOALLOC_BAD_ARGUMENT (-1)
 #define CATMSM_NOALLOC_TOO_LARGE (-2)

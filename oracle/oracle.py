@@ -26,11 +26,17 @@ _vp = C.c_void_p
 _sz = C.c_size_t
 
 
+# Where the reference sources are read from when the reference library is
+# built (BLST_REFERENCE_DIR; the default is this build machine's checkout).
+REFERENCE_DIR = os.environ.get("BLST_REFERENCE_DIR", "/root/reference")
+
+
 def build(ref=False):
-    """Compile liboracle.so (and the reference .so if asked and possible)."""
+    """Compile liboracle.so (and the reference .so if asked and the reference
+    sources are present)."""
     subprocess.run(["make", "-s", "-C", HERE], check=True)
-    if ref and os.path.isdir("/root/reference"):
-        subprocess.run(["make", "-s", "-C", HERE, "ref", "-j8"], check=True)
+    if ref and os.path.isdir(REFERENCE_DIR):
+        subprocess.run(["make", "-s", "-C", HERE, "ref", "-j8", "REF=" + REFERENCE_DIR], check=True)
 
 
 def _buf(data):
@@ -222,6 +228,22 @@ class Oracle(_Common):
 
     def on_curve(self, p: bytes) -> bool:
         return bool(self.L.op1_on_curve(_buf(p)))
+
+    def msm_seconds(self, points: bytes, scalars: bytes, n: int, nbits: int = 255):
+        """One whole contiguous-descriptor MSM call, timed around the C call
+        only (buffers prepared outside the timer); returns (seconds,
+        compressed result)."""
+        import time
+        pbuf, sbuf = _buf(bytearray(points)), _buf(bytearray(scalars))
+        parr = (C.c_void_p * 2)(C.cast(pbuf, C.c_void_p), None)
+        sarr = (C.c_void_p * 2)(C.cast(sbuf, C.c_void_p), None)
+        scratch = (C.c_uint64 * max(1, self.scratch_sizeof(n) // 8 + 1))()
+        ret = bytearray(P1)
+        rb = _buf(ret)
+        t = time.perf_counter()
+        self._msm(rb, parr, n, sarr, nbits, scratch)
+        el = time.perf_counter() - t
+        return el, self.compress(bytes(ret))
 
     def msm_raw(self, ret: bytearray, parr, n, sarr, nbits, scratch):
         self._msm(_buf(ret), parr, n, sarr, nbits, scratch)

@@ -328,7 +328,7 @@ static uint32_t enqueue_batch(const Basis* b, BatchWork* w, cudaStream_t st, uin
     k_fixup_seg<<<div_up(chunks, 128), 128, 0, st>>>((const uint32_t*)w->sorted_key.p, total, L, head);
     k_fixup_join<<<div_up(chunks, 128), 128, 0, st>>>((const uint32_t*)w->sorted_key.p, offsets, total, L, buckets,
                                                       head, tail, hot_list, hot_count);
-    k_fixup_hot_seg<<<2 * kSMs, 128, 0, st>>>(hot_list, hot_count, offsets, L, buckets, head, tail);
+    k_fixup_hot_seg<<<2 * device_sms(), 128, 0, st>>>(hot_list, hot_count, offsets, L, buckets, head, tail);
     fixup_giants(hot_list, hot_count, offsets, L, buckets, head, tail, true, st);
     xyzz* bufA[2] = {seg, seg + 2 * lvl1};
     xyzz* bufQ[2] = {seg + lvl1, seg + 2 * lvl1 + lvl2};

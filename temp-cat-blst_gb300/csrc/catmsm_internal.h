@@ -7,6 +7,13 @@ namespace catmsm {
 
 uint32_t msm_default_window(size_t n);
 
+// Bucket-count scan (k_scan_local / k_scan_top / k_scan_add in msm.cu): a
+// block of kScanThreads threads scans a tile of kScanTile counts, so M counts
+// need ceil(M / kScanTile) block sums.
+constexpr int kScanThreads = 1024;
+constexpr int kScanPer = 4;
+constexpr int kScanTile = kScanThreads * kScanPer;
+
 // Resident basis with fixed-base tables (batch.cu) and per-worker workspaces.
 struct Basis;
 struct BatchWork;

@@ -13,8 +13,24 @@
 
 namespace catmsm {
 
-// Number of SMs on a GB300 die pair; grids are sized in multiples of it.
-constexpr int kSMs = 152;
+// SMs of a GB300 (two dies of 76): used only by host-side plan models that
+// run without a device; launches size their grids from device_sms().
+constexpr int kGB300SMs = 152;
+
+// SM count of the current device, queried once per device (devices past the
+// cache are queried on every call); grids are sized in multiples of it.
+inline int device_sms()
+{
+    static int cache[64] = {0};
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess) dev = -1;
+    if (dev >= 0 && dev < 64 && cache[dev] > 0) return cache[dev];
+    int sms = 0;
+    if (dev < 0 || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
+        return kGB300SMs;   // only reached with a broken context; the next launch reports the error
+    if (dev < 64) cache[dev] = sms;
+    return sms;
+}
 
 struct DevBuf {
     void* p = nullptr;

@@ -221,7 +221,7 @@ static size_t fft_quad_max()
     int sms = 0, per_sm = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fft_stage_multi<true>, 64, 0);
-    size_t v = (sms > 0 && per_sm > 0) ? (size_t)sms * per_sm * 64 / 4 : (size_t)kSMs * 64;
+    size_t v = (sms > 0 && per_sm > 0) ? (size_t)sms * per_sm * 64 / 4 : (size_t)device_sms() * 64;
     if (dev >= 0 && dev < 64) by_dev[dev] = v;
     return v;
 }

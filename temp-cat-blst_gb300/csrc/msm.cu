@@ -242,9 +242,6 @@ __global__ void k_tile_digits(const uint8_t* __restrict__ scalars, uint32_t stri
 }
 
 // ----------------------------------------------------------------- 2. scan
-constexpr int kScanThreads = 1024;
-constexpr int kScanPer = 4;
-constexpr int kScanTile = kScanThreads * kScanPer;
 
 __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* smem_warp, uint32_t* total)
 {
@@ -739,12 +736,12 @@ void fixup_giants(const void* hot_list, const uint32_t* hot_count, const uint32_
 {
     const uint2* hl = (const uint2*)hot_list;
     if (seg) {
-        k_fixup_giant<true><<<2 * kSMs, kHotThreads, 0, st>>>(hl, hot_count, offsets, L, (xyzz*)head, (xyzz*)tail);
-        k_fixup_giant_join<true><<<2 * kSMs, kHotThreads, 0, st>>>(hl, hot_count, offsets, L, (xyzz*)buckets,
+        k_fixup_giant<true><<<2 * device_sms(), kHotThreads, 0, st>>>(hl, hot_count, offsets, L, (xyzz*)head, (xyzz*)tail);
+        k_fixup_giant_join<true><<<2 * device_sms(), kHotThreads, 0, st>>>(hl, hot_count, offsets, L, (xyzz*)buckets,
                                                                    (xyzz*)head, (xyzz*)tail);
     } else {
-        k_fixup_giant<false><<<2 * kSMs, kHotThreads, 0, st>>>(hl, hot_count, offsets, L, (xyzz*)head, (xyzz*)tail);
-        k_fixup_giant_join<false><<<2 * kSMs, kHotThreads, 0, st>>>(hl, hot_count, offsets, L, (xyzz*)buckets,
+        k_fixup_giant<false><<<2 * device_sms(), kHotThreads, 0, st>>>(hl, hot_count, offsets, L, (xyzz*)head, (xyzz*)tail);
+        k_fixup_giant_join<false><<<2 * device_sms(), kHotThreads, 0, st>>>(hl, hot_count, offsets, L, (xyzz*)buckets,
                                                                     (xyzz*)head, (xyzz*)tail);
     }
 }
@@ -996,7 +993,7 @@ static uint32_t accumulate_chunk(size_t nD)
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_accumulate, 128, 0);
         if (sms <= 0 || per_sm <= 0) {
-            sms = kSMs;
+            sms = device_sms();
             per_sm = 4;
         }
         slots = sms * per_sm * 128;
@@ -1188,15 +1185,15 @@ static cudaError_t msm_run(Ctx* ctx, const void* d_points, const uint8_t* d_scal
         k_fixup_seg<<<div_up(chunks, 128), 128, 0, st>>>(sorted_key, total, L, head);
         k_fixup_join<<<div_up(chunks, 128), 128, 0, st>>>(sorted_key, offsets, total, L, buckets, head, tail,
                                                           hot_list, hot_count);
-        k_fixup_hot_seg<<<2 * kSMs, kHotThreads, 0, st>>>(hot_list, hot_count, offsets, L, buckets, head, tail);
+        k_fixup_hot_seg<<<2 * device_sms(), kHotThreads, 0, st>>>(hot_list, hot_count, offsets, L, buckets, head, tail);
         fixup_giants(hot_list, hot_count, offsets, L, buckets, head, tail, true, st);
         g_stats.launches += 3;
     } else {
         // short spans: one thread joins each bucket's few carries
         k_fixup<<<div_up(chunks, 128), 128, 0, st>>>(sorted_key, offsets, total, L, buckets, head, tail, hot_list,
                                                      hot_count, (uint32_t)chunks);
-        k_fixup_hot<<<2 * kSMs, kHotThreads, 0, st>>>(hot_list, hot_count, offsets, L, buckets, head, tail);
-        k_fixup_rest<<<2 * kSMs, 128, 0, st>>>(hot_list, hot_count, (uint32_t)chunks, offsets, L, buckets, head);
+        k_fixup_hot<<<2 * device_sms(), kHotThreads, 0, st>>>(hot_list, hot_count, offsets, L, buckets, head, tail);
+        k_fixup_rest<<<2 * device_sms(), 128, 0, st>>>(hot_list, hot_count, (uint32_t)chunks, offsets, L, buckets, head);
         fixup_giants(hot_list, hot_count, offsets, L, buckets, head, tail, false, st);
         g_stats.launches += 3;
     }

@@ -20,8 +20,17 @@
 //  * calls that overlap on the GPU (from several host threads, or on several
 //    streams) race on the shared array and give wrong results: serialise them;
 //  * the first call on each device looks up the array's device address
-//    (cudaGetSymbolAddress) with that device current; make that first call
-//    before any stream capture.
+//    (cudaGetSymbolAddress) with that device current.  With the CUDA
+//    runtime's default lazy module loading, that lookup is also the moment
+//    the device reserves the array: make the first call on each device early,
+//    before another framework claims the GPU's memory (or it can fail with an
+//    out-of-memory error although the call itself allocates nothing) and
+//    before any stream capture;
+//  * devices are indexed 0..63 (a call on a device with a higher index
+//    returns cudaErrorInvalidDevice);
+//  * a call that fails after queueing work waits for that work before it
+//    returns, so a caller that serialises calls on the host never overlaps
+//    them on the GPU.
 // The kernels are the regular pipeline's (msm.cu); only the workspace differs.
 #include "common.cuh"
 #include "curve.cuh"
@@ -80,7 +89,6 @@ constexpr size_t kChunks = (kND + kL - 1) / kL;
 static_assert(kMaxPoints / kL + 1 <= 1024, "noalloc buckets must stay within the block join");
 constexpr size_t kLvl1 = (size_t)kMaxD * (kB / 8);
 constexpr size_t kLvl2 = (size_t)kMaxD * (kB / 16) + kMaxD;
-constexpr int kScanTileNa = 1024 * 4;   // k_scan_local's tile (1024 threads x 4)
 
 constexpr size_t al(size_t x) { return (x + 255) & ~(size_t)255; }
 
@@ -92,7 +100,7 @@ constexpr size_t oRanks = oDigits + al(kND * 4);
 constexpr size_t oCounts = oRanks + al(kND * 4);
 constexpr size_t oOffsets = oCounts + al(kM * 4);
 constexpr size_t oBsums = oOffsets + al((kM + 1) * 4);
-constexpr size_t oSortedPt = oBsums + al(((kM + kScanTileNa - 1) / kScanTileNa) * 4);
+constexpr size_t oSortedPt = oBsums + al(((kM + kScanTile - 1) / kScanTile) * 4);
 constexpr size_t oSortedKey = oSortedPt + al(kND * 4);
 constexpr size_t oBuckets = oSortedKey + al(kND * 4);
 constexpr size_t oHead = oBuckets + al(kM * sizeof(xyzz));
@@ -126,18 +134,17 @@ static cudaError_t noalloc_setup(unsigned char** out)
     return cudaSuccess;
 }
 
-static cudaError_t noalloc_run(const blst_p1_affine* points, const blst_byte* scalars, size_t n, uint32_t nbits,
-                               uint64_t out[18])
+// Queues the whole pipeline on st; the D window sums land in h_wins once st
+// is synchronised.
+static cudaError_t noalloc_queue(unsigned char* base, const blst_p1_affine* points, const blst_byte* scalars,
+                                 size_t n, uint32_t nbits, cudaStream_t st, uint64_t* h_wins)
 {
-    unsigned char* base = nullptr;
-    CATMSM_CHECK(noalloc_setup(&base));
-    cudaStream_t st = cudaStreamPerThread;
     const uint32_t D = nbits / kC + 1;
     const size_t M = (size_t)D * kB;
     const size_t nD = n * D;
     const size_t chunks = (nD + kL - 1) / kL;
     const uint32_t nbytes = (nbits + 7) / 8;
-    const uint32_t nblocks = (uint32_t)((M + kScanTileNa - 1) / kScanTileNa);
+    const uint32_t nblocks = (uint32_t)((M + kScanTile - 1) / kScanTile);
 
     affine* d_pts = reinterpret_cast<affine*>(base + oPoints);
     uint8_t* d_sc = base + oScalars;
@@ -164,16 +171,16 @@ static cudaError_t noalloc_run(const blst_p1_affine* points, const blst_byte* sc
     CATMSM_CHECK(cudaMemsetAsync(buckets, 0, M * sizeof(xyzz), st));
     CATMSM_CHECK(cudaMemsetAsync(hot_count, 0, 12, st));
     k_digits<<<div_up(n, 256), 256, 0, st>>>(d_sc, nbytes, (uint32_t)n, nbits, kC, D, digits, ranks, counts);
-    k_scan_local<<<nblocks, 1024, 0, st>>>(counts, offsets, bsums, (uint32_t)M);
-    k_scan_top<<<1, 1024, 0, st>>>(bsums, nblocks, total);
+    k_scan_local<<<nblocks, kScanThreads, 0, st>>>(counts, offsets, bsums, (uint32_t)M);
+    k_scan_top<<<1, kScanThreads, 0, st>>>(bsums, nblocks, total);
     k_scan_add<<<div_up(M, 256), 256, 0, st>>>(offsets, bsums, (uint32_t)M);
     k_scatter<<<div_up(nD, 256), 256, 0, st>>>(digits, ranks, offsets, (uint32_t)n, (uint32_t)nD, sorted_pt,
                                               sorted_key);
     k_accumulate<<<div_up(chunks, 128), 128, 0, st>>>(d_pts, sorted_pt, sorted_key, total, kL, buckets, head, tail);
     k_fixup<<<div_up(chunks, 128), 128, 0, st>>>(sorted_key, offsets, total, kL, buckets, head, tail, hot_list,
                                                  hot_count, (uint32_t)kChunks);
-    k_fixup_hot<<<kSMs, 128, 0, st>>>(hot_list, hot_count, offsets, kL, buckets, head, tail);
-    k_fixup_rest<<<kSMs, 128, 0, st>>>(hot_list, hot_count, (uint32_t)kChunks, offsets, kL, buckets, head);
+    k_fixup_hot<<<device_sms(), 128, 0, st>>>(hot_list, hot_count, offsets, kL, buckets, head, tail);
+    k_fixup_rest<<<device_sms(), 128, 0, st>>>(hot_list, hot_count, (uint32_t)kChunks, offsets, kL, buckets, head);
     xyzz* bufA[2] = {seg, seg + 2 * kLvl1};
     xyzz* bufQ[2] = {seg + kLvl1, seg + 2 * kLvl1 + kLvl2};
     const xyzz* inA = buckets;
@@ -193,9 +200,24 @@ static cudaError_t noalloc_run(const blst_p1_affine* points, const blst_byte* sc
     }
     CATMSM_CHECK(cudaMemcpyAsync(wins, inQ, (size_t)D * sizeof(xyzz), cudaMemcpyDeviceToDevice, st));
     CATMSM_CHECK(cudaGetLastError());
-    uint64_t h_wins[kMaxD * 24];
     CATMSM_CHECK(cudaMemcpyAsync(h_wins, wins, (size_t)D * sizeof(xyzz), cudaMemcpyDeviceToHost, st));
-    CATMSM_CHECK(cudaStreamSynchronize(st));
+    return cudaSuccess;
+}
+
+static cudaError_t noalloc_run(const blst_p1_affine* points, const blst_byte* scalars, size_t n, uint32_t nbits,
+                               uint64_t out[18])
+{
+    unsigned char* base = nullptr;
+    CATMSM_CHECK(noalloc_setup(&base));
+    cudaStream_t st = cudaStreamPerThread;
+    const uint32_t D = nbits / kC + 1;
+    uint64_t h_wins[kMaxD * 24];
+    const cudaError_t qerr = noalloc_queue(base, points, scalars, n, nbits, st, h_wins);
+    // wait also when queueing failed part-way: work already queued may still
+    // be using the shared array, and the next call must not overlap it
+    const cudaError_t serr = cudaStreamSynchronize(st);
+    if (qerr != cudaSuccess) return qerr;
+    CATMSM_CHECK(serr);
 
     using namespace catmsm_host;
     hjac ret;

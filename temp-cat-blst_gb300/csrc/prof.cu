@@ -61,7 +61,7 @@ static double imad_run(bool wide)
 {
     Ctx* ctx = get_ctx();
     if (!ctx) return -1.0;
-    int sms = kSMs;
+    int sms = device_sms();
     int dev = 0;
     if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int blocks = 8 * sms, threads = 256;

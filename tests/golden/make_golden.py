@@ -24,9 +24,26 @@ reference's own C ABI built from its sources (oracle/_ref/libblst_ref.so):
             entry in oracle/ref_shim.cpp) -> sha256 of blst_p1_serialize of
             every element, per (seed, n, xn); each equals the full transform
 
-`--section wbits|msm_fr_variants|tile|fft_truncated` regenerates only that section of an
-existing file.
+  * msm_large: the large-MSM workload's other scalar distributions at 2^20
+            and 2^22 (64-bit scalars at nbits = 255 and packed at nbits = 64;
+            10% zero scalars with 5% duplicated points), appended to msm
+  * fft_large: G1 FFT at 2^14 and 2^16 in all five modes, appended to fft
+  * batch_commitments: the batched-commitments workload (1024 commitments,
+            k_j = floor(2^U), U ~ U[8, 12] from numpy's default_rng(3), over
+            the 4096-point basis P_i = k_i G with k = synth.point_scalars(3),
+            scalars synth.scalars(3003)): blst_p1s_mult_pippenger over the
+            first k_j basis points -> compressed, every commitment
+  * bench_fft: the batched-FFT workload's inputs (the first n points of
+            synth.point_scalars(4, 2^16) as Jacobian with z = 1, prepared
+            domains) -> sha256 of the forward and inverse outputs per size
+
+`--section wbits|msm_fr_variants|tile|fft_truncated|msm_large|fft_large|batch_commitments|bench_fft`
+regenerates only that section of an existing file (msm_large and fft_large
+replace their own cases inside msm and fft).  The large sections run their
+reference calls on a thread pool (ctypes releases the GIL; the reference has
+no global mutable state).
 """
+import concurrent.futures as cf
 import hashlib
 import json
 import os
@@ -161,6 +178,125 @@ def fft_truncated_section(o, r):
     return out
 
 
+MSM_LARGE_CASES = [
+    # (seed, n, kind, nbits, dup): the large-MSM workload's distributions (b) and (c)
+    (25, 1 << 20, 1, 255, False), (26, 1 << 20, 1, 64, False), (27, 1 << 20, 2, 255, True),
+    (28, 1 << 22, 1, 255, False), (29, 1 << 22, 1, 64, False), (30, 1 << 22, 2, 255, True),
+]
+FFT_LARGE_CASES = [(46, 1 << 14), (47, 1 << 16)]
+FFT_MODES = ("fwd", "inv", "dfwd", "dinv", "dunscaled")
+_THREADS = max(1, os.cpu_count() or 1)
+
+
+def _fft_mode(r, jac, n, d, mode):
+    if mode == "fwd":
+        return r.p1_fft(jac, n, False)
+    if mode == "inv":
+        return r.p1_fft(jac, n, True)
+    if mode == "dfwd":
+        return r.p1_fft_with_domain(jac, n, d, n + 2, False)
+    if mode == "dinv":
+        return r.p1_fft_with_domain(jac, n, d, n + 2, True)
+    return r.p1_ifft_unscaled_with_domain(jac, n, d, n + 2)
+
+
+def msm_large_section(o, r):
+    """Reference MSMs of MSM_LARGE_CASES, several at once."""
+    def one(case):
+        seed, n, kind, nbits, dup = case
+        t = time.time()
+        pts, sc = msm_inputs(o, seed, n, kind, nbits, dup)
+        res = r.msm(pts, sc, n, nbits)
+        print("msm_large", seed, n, kind, nbits, dup, res.hex()[:16], "%.1fs" % (time.time() - t), flush=True)
+        return {"seed": seed, "n": n, "kind": kind, "nbits": nbits, "dup": dup, "compressed": res.hex()}
+    with cf.ThreadPoolExecutor(max_workers=3) as ex:
+        return list(ex.map(one, MSM_LARGE_CASES))
+
+
+def fft_large_section(o, r):
+    """Reference G1 FFTs of FFT_LARGE_CASES in all five modes, in parallel."""
+    inputs = {}
+    for seed, n in FFT_LARGE_CASES:
+        inputs[(seed, n)] = (o.jacobian_randomize(seed, n, o.gen_points(seed, n)), r.domain(n))
+
+    def one(job):
+        (seed, n), mode = job
+        t = time.time()
+        jac, d = inputs[(seed, n)]
+        ok, out = _fft_mode(r, jac, n, d, mode)
+        assert ok
+        ser = b"".join(r.serialize(out[144 * i:144 * i + 144]) for i in range(n))
+        print("fft_large", seed, n, mode, "%.1fs" % (time.time() - t), flush=True)
+        return {"seed": seed, "n": n, "mode": mode, "sha256": hashlib.sha256(ser).hexdigest()}
+    jobs = [(c, m) for c in FFT_LARGE_CASES for m in FFT_MODES]
+    with cf.ThreadPoolExecutor(max_workers=_THREADS) as ex:
+        return list(ex.map(one, jobs))
+
+
+def batch_commitments_inputs(o):
+    """The batched-commitments workload: (counts, basis points, scalars)."""
+    import numpy as np
+    synth = _synth()
+    nb, nmsm, seed = 4096, 1024, 3
+    rng = np.random.default_rng(seed)
+    counts = [int(2 ** u) for u in rng.uniform(8, 12, nmsm)]
+    pts = o.points_from_scalars(synth.point_scalars(seed, nb), nb)
+    sc = synth.scalars(seed + 3000, sum(counts), 0)
+    return counts, pts, sc
+
+
+def batch_commitments_section(o, r):
+    counts, pts, sc = batch_commitments_inputs(o)
+    offs = [0]
+    for k in counts:
+        offs.append(offs[-1] + k)
+
+    def one(j):
+        k = counts[j]
+        return r.msm(pts[:96 * k], sc[32 * offs[j]:32 * offs[j + 1]], k, 256).hex()
+    t = time.time()
+    with cf.ThreadPoolExecutor(max_workers=_THREADS) as ex:
+        res = list(ex.map(one, range(len(counts))))
+    print("batch_commitments", len(res), "%.1fs" % (time.time() - t), flush=True)
+    return {"n_basis": 4096, "seed": 3, "nbits": 256, "counts": counts, "compressed": res,
+            "sha256": hashlib.sha256(b"".join(bytes.fromhex(x) for x in res)).hexdigest()}
+
+
+def bench_fft_section(o, r):
+    synth = _synth()
+    big = 1 << 16
+    aff = o.points_from_scalars(synth.point_scalars(4, big), big)
+    one_m = ((1 << 384) % 0x1a0111ea397fe69a4b1ba7b6434bacd764774b84f38512bf6730d2a0f6b0f6241eabfffeb153ffffb9feffffffffaaab
+             ).to_bytes(48, "little")
+
+    def one(job):
+        n, inverse = job
+        t = time.time()
+        jac = b"".join(aff[96 * i:96 * i + 96] + one_m for i in range(n))
+        ok, out = r.p1_fft_with_domain(jac, n, r.domain(n), n + 2, inverse)
+        assert ok
+        ser = b"".join(r.serialize(out[144 * i:144 * i + 144]) for i in range(n))
+        print("bench_fft", n, inverse, "%.1fs" % (time.time() - t), flush=True)
+        return {"n": n, "mode": "dinv" if inverse else "dfwd", "sha256": hashlib.sha256(ser).hexdigest()}
+    jobs = [(1 << e, inv) for e in (10, 12, 14, 16) for inv in (False, True)]
+    with cf.ThreadPoolExecutor(max_workers=_THREADS) as ex:
+        return {"seed": 4, "z": 1, "cases": list(ex.map(one, jobs))}
+
+
+def _synth():
+    import importlib.util
+    path = os.path.join(ROOT, "temp-cat-blst_gb300", "synth.py")
+    spec = importlib.util.spec_from_file_location("catmsm_synth", path)
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def _replace_cases(old, new, key):
+    have = {key(c) for c in new}
+    return [c for c in old if key(c) not in have] + new
+
+
 def main():
     large = "--large" in sys.argv
     build(ref=True)
@@ -168,8 +304,14 @@ def main():
     if "--section" in sys.argv:
         name = sys.argv[sys.argv.index("--section") + 1]
         g = json.load(open(OUT))
-        g[name] = {"wbits": wbits_section, "msm_fr_variants": fr_variants_section, "tile": tile_section,
-                   "fft_truncated": fft_truncated_section}[name](o, r)
+        if name == "msm_large":
+            g["msm"] = _replace_cases(g["msm"], msm_large_section(o, r), lambda c: (c["seed"], c["n"]))
+        elif name == "fft_large":
+            g["fft"] = _replace_cases(g["fft"], fft_large_section(o, r), lambda c: (c["seed"], c["n"], c["mode"]))
+        else:
+            g[name] = {"wbits": wbits_section, "msm_fr_variants": fr_variants_section, "tile": tile_section,
+                       "fft_truncated": fft_truncated_section, "batch_commitments": batch_commitments_section,
+                       "bench_fft": bench_fft_section}[name](o, r)
         json.dump(g, open(OUT, "w"), indent=1)
         print("wrote", OUT)
         return
@@ -253,13 +395,21 @@ def main():
     g["msm_fr_variants"] = fr_variants_section(o, r)
     g["tile"] = tile_section(o, r)
     g["fft_truncated"] = fft_truncated_section(o, r)
-    if not large and os.path.exists(OUT):
-        # keep previously generated large cases
+    if large:
+        g["msm"] += msm_large_section(o, r)
+        g["fft"] += fft_large_section(o, r)
+        g["batch_commitments"] = batch_commitments_section(o, r)
+        g["bench_fft"] = bench_fft_section(o, r)
+    elif os.path.exists(OUT):
+        # keep previously generated large cases and sections
         old = json.load(open(OUT))
         have = {(c["seed"], c["n"]) for c in g["msm"]}
         g["msm"] += [c for c in old["msm"] if (c["seed"], c["n"]) not in have]
         havef = {(c["seed"], c["n"], c["mode"]) for c in g["fft"]}
         g["fft"] += [c for c in old["fft"] if (c["seed"], c["n"], c["mode"]) not in havef]
+        for name in ("batch_commitments", "bench_fft"):
+            if name in old:
+                g[name] = old[name]
     json.dump(g, open(OUT, "w"), indent=1)
     print("wrote", OUT)
 

@@ -61,3 +61,22 @@ def test_reference_arm_other_ranks_exit_clean():
         steps = 1
         warmup = 0
     assert b.run_reference(A(), 2, 1) == 0
+
+
+def test_bench_affine_encodings_match_oracle():
+    """bench.py checks GPU outputs against the reference's golden bytes with
+    its own Python normalisation and encodings (one batched inversion);
+    they must equal the oracle's blst_p1_compress / blst_p1_serialize,
+    including infinity and non-unit z."""
+    import oracle as om
+    b = _bench()
+    o = om.Oracle()
+    n = 40
+    jac = o.jacobian_randomize(9, n, o.gen_points(9, n))
+    blobs = [jac[144 * i:144 * i + 144] for i in range(n)]
+    blobs[3] = bytes(144)                                  # infinity (z = 0)
+    xys = b._affine_many(blobs)
+    assert xys[3] is None
+    for blob, xy in zip(blobs, xys):
+        assert b._compress_xy(xy) == o.compress(blob)
+        assert b._serialize_xy(xy) == o.serialize(blob)

@@ -79,3 +79,28 @@ def test_batch_autotune_persists(gpu, oracle, synth, tmp_path, monkeypatch):
     assert b.autotune(counts, sc) == (w, c)          # served from the cache
     _check(oracle, pts, counts, sc, b.msm_batch(counts, sc))
     b.close()
+
+
+def test_batch_commitments_match_reference_golden(gpu, oracle, synth, golden):
+    """The batched-commitments workload itself: 1024 commitments over the
+    4096-point basis (k_j = floor(2^U), U ~ U[8, 12]), every result against
+    the reference's own blst_p1s_mult_pippenger output, with the library's
+    default (window, chunk) and with the (11, 96) the autotuner picks for this
+    batch on a GB300."""
+    import numpy as np
+    g = golden["batch_commitments"]
+    nb, seed = g["n_basis"], g["seed"]
+    counts = g["counts"]
+    rng = np.random.default_rng(seed)
+    assert [int(2 ** u) for u in rng.uniform(8, 12, len(counts))] == counts
+    pts = gpu.points_from_scalars(synth.point_scalars(seed, nb), nb)
+    sc = synth.scalars(seed + 3000, sum(counts), 0)
+    b = gpu.Basis(pts, nb)
+    for cfg in (None, (11, 96)):
+        if cfg:
+            b.set_config(*cfg)
+        out = b.msm_batch(counts, sc)
+        got = [oracle.compress(out[144 * j:144 * j + 144]).hex() for j in range(len(counts))]
+        bad = [j for j in range(len(counts)) if got[j] != g["compressed"][j]]
+        assert not bad, (cfg, bad[:8])
+    b.close()

@@ -251,3 +251,30 @@ def test_fft_batch_rejects_before_writing(gpu, oracle):
     assert rc != 0 and outs == [jac, jac]
     rc, outs = gpu.p1_fft_batch([jac], [n], [d], [3])
     assert rc != 0 and outs == [jac]
+
+
+def test_fft_batch_workload_golden(gpu, oracle, golden, synth):
+    """The batched-FFT workload's inputs (the first n points of the seeded
+    2^16-point set as Jacobian with z = 1, prepared domains) for n = 2^10 ..
+    2^16, forward and inverse in ONE batch, against the reference's
+    blst_p1_fft_with_domain output (sha256 of every element's serialization)."""
+    g = golden["bench_fft"]
+    big = 1 << 16
+    aff = gpu.points_from_scalars(synth.point_scalars(g["seed"], big), big)
+    P = 0x1a0111ea397fe69a4b1ba7b6434bacd764774b84f38512bf6730d2a0f6b0f6241eabfffeb153ffffb9feffffffffaaab
+    one = ((1 << 384) % P).to_bytes(48, "little")
+    cases = g["cases"]
+    vals, ns, doms, modes = [], [], [], []
+    for c in cases:
+        n = c["n"]
+        vals.append(b"".join(aff[96 * i:96 * i + 96] + one for i in range(n)))
+        ns.append(n)
+        ok, d = gpu.fr_fft_domain_init(n)
+        assert ok
+        doms.append(d)
+        modes.append(1 if c["mode"] == "dinv" else 0)
+    rc, outs = gpu.p1_fft_batch(vals, ns, doms, modes)
+    assert rc == 0
+    for c, n, out in zip(cases, ns, outs):
+        ser = b"".join(oracle.serialize(out[144 * i:144 * i + 144]) for i in range(n))
+        assert hashlib.sha256(ser).hexdigest() == c["sha256"], (n, c["mode"])
