@@ -250,6 +250,12 @@ int catmsm_msm_plan_detail(size_t npoints, size_t nbits, int glv, size_t *window
  * without a device context.  Both settings give the same group element for
  * subgroup points, the reference's precondition. */
 int catmsm_msm_glv(int enable);
+/* Batch-affine accumulation rounds of this thread's MSMs (no reference
+ * counterpart): 0 = XYZZ mixed additions only, 1..8 = that many rounds of
+ * affine additions behind Montgomery batch inversions before the XYZZ fold,
+ * -1 = chosen by size (the default).  Returns the previous setting (-2 if no
+ * device context); values outside -1..8 only query. */
+int catmsm_msm_affine_rounds(int rounds);
 
 /* Seeded-input support: out[i] = k_i * G (affine, canonical) for n 32-byte
  * little-endian scalars.  Host buffers; returns 0 on success. */
@@ -368,6 +374,10 @@ int catmsm_p1s_affine_in_g1(const blst_p1_affine *points, size_t n, int *results
  * buffers of n blst_fp with inputs below 2p; a == b (the same pointer)
  * selects the dedicated squaring.  Returns 0 on success. */
 int catmsm_fp_mul(blst_fp *out, const blst_fp *a, const blst_fp *b, size_t n);
+/* Field self-check of the batch-affine rounds' inversion: out[i] = a[i]^-1
+ * in Montgomery form (canonical; zero maps to zero), host buffers of n
+ * blst_fp with inputs below 2p.  Returns 0 on success. */
+int catmsm_fp_inv(blst_fp *out, const blst_fp *a, size_t n);
 
 #ifdef __cplusplus
 }

@@ -91,6 +91,10 @@ def load(build_if_missing=True):
     L.catmsm_msm_plan_detail.argtypes = [_sz, _sz, C.c_int, _vp, _vp, _vp, _vp, _vp]
     L.catmsm_msm_glv.restype = C.c_int
     L.catmsm_msm_glv.argtypes = [C.c_int]
+    L.catmsm_msm_affine_rounds.restype = C.c_int
+    L.catmsm_msm_affine_rounds.argtypes = [C.c_int]
+    L.catmsm_fp_inv.restype = C.c_int
+    L.catmsm_fp_inv.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t]
     L.catmsm_p1_affines_from_scalars.restype = C.c_int
     L.catmsm_p1_affines_from_scalars.argtypes = [_vp, _vp, _sz]
     L.catmsm_p1_affines_from_scalars_device.restype = C.c_int
@@ -461,6 +465,22 @@ def msm_plan_detail(n: int, nbits: int = 255, glv: int = 1):
 def msm_glv(enable: int = -1) -> int:
     """Set (0/1) or query (-1) the GLV split for this thread; returns the previous setting."""
     return load().catmsm_msm_glv(enable)
+
+
+def msm_affine_rounds(rounds: int = -2) -> int:
+    """Set (-1 = by size, 0..8) or query (-2) this thread's batch-affine
+    accumulation rounds; returns the previous setting."""
+    return load().catmsm_msm_affine_rounds(rounds)
+
+
+def fp_inv(a: bytes, n: int) -> bytes:
+    """Montgomery-form inverses of n field elements (0 -> 0) on the device
+    (the variable-time inversion of the batch-affine rounds)."""
+    out = bytearray(48 * n)
+    rc = load().catmsm_fp_inv(_buf(out), _buf(a), n)
+    if rc != 0:
+        raise RuntimeError("catmsm_fp_inv failed: %d" % rc)
+    return bytes(out)
 
 
 def imad_peak_tera() -> float:

@@ -439,6 +439,15 @@ int catmsm_msm_glv(int enable)
     return prev;
 }
 
+int catmsm_msm_affine_rounds(int rounds)
+{
+    Ctx* ctx = get_ctx();
+    if (!ctx) return -2;
+    const int prev = ctx->affine_rounds;
+    if (rounds >= -1 && rounds <= 8) ctx->affine_rounds = rounds;
+    return prev;
+}
+
 int catmsm_msm_plan_detail(size_t npoints, size_t nbits, int glv, size_t* window, size_t* windows, size_t* points,
                            size_t* chunk, size_t* fan_in)
 {
@@ -489,6 +498,22 @@ int catmsm_p1_affines_from_scalars(blst_p1_affine* out, const blst_byte* k32, si
     if (err == cudaSuccess) err = points_from_scalars_device(ctx, (const uint8_t*)dk, n, dp);
     if (err == cudaSuccess)
         err = cudaMemcpyAsync(out, dp, sizeof(blst_p1_affine) * n, cudaMemcpyDeviceToHost, ctx->stream);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(ctx->stream);
+    return (int)err;
+}
+
+int catmsm_fp_inv(blst_fp* out, const blst_fp* a, size_t n)
+{
+    if (n == 0) return 0;
+    if (!out || !a) return (int)cudaErrorInvalidValue;
+    Ctx* ctx = get_ctx();
+    if (!ctx) return (int)cudaErrorInitializationError;
+    uint64_t* d = (uint64_t*)ctx->msm.digits.get(2 * n * sizeof(blst_fp));
+    if (!d) return (int)cudaErrorMemoryAllocation;
+    cudaError_t err = cudaMemcpyAsync(d, a, n * sizeof(blst_fp), cudaMemcpyHostToDevice, ctx->stream);
+    if (err == cudaSuccess) err = fp_inv_test_device(ctx, d, d + 6 * n, n);
+    if (err == cudaSuccess)
+        err = cudaMemcpyAsync(out, d + 6 * n, n * sizeof(blst_fp), cudaMemcpyDeviceToHost, ctx->stream);
     if (err == cudaSuccess) err = cudaStreamSynchronize(ctx->stream);
     return (int)err;
 }

@@ -50,6 +50,17 @@ void fixup_giants(const void* hot_list, const uint32_t* hot_count, const uint32_
 void msm_reduce_pair(const void* inA, const void* inQ, uint32_t m, uint32_t D, void* outA, void* outQ,
                      cudaStream_t st);
 
+// Bucket accumulation with `rounds` rounds of batch-affine additions
+// (Montgomery batch inversion per block and round) before the XYZZ fold;
+// same outputs as k_accumulate (buckets / head / tail per chunk of L sorted
+// entries), so the fixup stage is unchanged.
+cudaError_t msm_accumulate_affine(Ctx* ctx, const void* pts, const uint32_t* sorted_pt, const uint32_t* sorted_key,
+                                  const uint32_t* total, uint32_t L, size_t chunks, uint32_t rounds, void* buckets,
+                                  void* head, void* tail, cudaStream_t st);
+// Rounds the plain MSM uses for nD bucket entries over M buckets (0: the
+// XYZZ-only k_accumulate).
+uint32_t msm_affine_rounds(size_t nD, size_t M);
+
 // H2D of `bytes` from src to dst on the context's copy stream, after the work
 // already queued on its pipeline stream; *ready is an event recorded after
 // the copy (pass it to msm_device as points_ready).
@@ -65,6 +76,10 @@ cudaError_t msm_tile_device(Ctx* ctx, const void* d_points, const uint8_t* d_sca
                             uint32_t nbits, uint32_t bit0, uint32_t window, uint64_t* out);
 
 cudaError_t points_from_scalars_device(Ctx* ctx, const uint8_t* d_k32, size_t n, void* d_out);
+
+// d_out[i] = d_a[i]^-1 (Montgomery form, canonical; 0 -> 0) by the
+// variable-time inversion of the batch-affine rounds.
+cudaError_t fp_inv_test_device(Ctx* ctx, const uint64_t* d_a, uint64_t* d_out, size_t n);
 
 cudaError_t fp_mul_test_device(Ctx* ctx, const uint64_t* d_a, const uint64_t* d_b, uint64_t* d_out, size_t n,
                                bool square);

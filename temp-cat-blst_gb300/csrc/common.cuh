@@ -82,6 +82,8 @@ struct PinnedBuf {
 struct MsmWork {
     DevBuf points, scalars, digits, ranks, counts, offsets, block_sums, sorted_pt, sorted_key,
         buckets, head, tail, seg, wins, total, status, misc, glv_pts, glv_sc, glv_sign;
+    // batch-affine accumulation rounds (bucket_affine.cu)
+    DevBuf aff_pts0, aff_pts1, aff_key0, aff_key1, aff_meta, aff_pairpos, aff_prefix, aff_ttot, aff_btot;
 };
 
 struct FftWork {
@@ -106,8 +108,12 @@ struct Ctx {
     PinnedBuf h_points, h_scalars, h_out, h_values, h_meta;
     StageProfile prof;
     bool glv = true;   // GLV split of scalars wider than 128 bits (catmsm_msm_glv)
+    int affine_rounds = -1;   // batch-affine accumulation rounds (-1: by size; catmsm_msm_affine_rounds)
     cudaStream_t copy_stream = nullptr;    // host->device point copies that overlap the scalar stages
     cudaEvent_t points_ready = nullptr;
+    // second half of the batch-affine rounds (bucket_affine.cu), forked from and joined to `stream`
+    cudaStream_t aff_stream = nullptr;
+    cudaEvent_t aff_fork = nullptr, aff_join = nullptr;
 };
 
 // Per-thread context bound to the thread's current device.

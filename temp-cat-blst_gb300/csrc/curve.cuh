@@ -22,6 +22,49 @@ struct affine { fp x, y; };
 struct jac { fp x, y, z; };
 struct xyzz { fp x, y, zz, zzz; };
 
+// Vectorised global loads and stores of points (16-byte aligned rows).
+__device__ __forceinline__ void load_affine(fp& x, fp& y, const affine* p)
+{
+    const uint4* q = reinterpret_cast<const uint4*>(p);
+    uint4 v[6];
+#pragma unroll
+    for (int k = 0; k < 6; k++) v[k] = __ldg(q + k);
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        x.v[4 * k + 0] = v[k].x; x.v[4 * k + 1] = v[k].y;
+        x.v[4 * k + 2] = v[k].z; x.v[4 * k + 3] = v[k].w;
+        y.v[4 * k + 0] = v[k + 3].x; y.v[4 * k + 1] = v[k + 3].y;
+        y.v[4 * k + 2] = v[k + 3].z; y.v[4 * k + 3] = v[k + 3].w;
+    }
+}
+
+__device__ __forceinline__ void store_xyzz(xyzz* dst, const xyzz& p)
+{
+    uint4* q = reinterpret_cast<uint4*>(dst);
+    const uint32_t* s = reinterpret_cast<const uint32_t*>(&p);
+#pragma unroll
+    for (int k = 0; k < 12; k++) q[k] = make_uint4(s[4 * k], s[4 * k + 1], s[4 * k + 2], s[4 * k + 3]);
+}
+
+__device__ __forceinline__ void store_affine(affine* dst, const affine& p)
+{
+    uint4* q = reinterpret_cast<uint4*>(dst);
+    const uint32_t* s = reinterpret_cast<const uint32_t*>(&p);
+#pragma unroll
+    for (int k = 0; k < 6; k++) q[k] = make_uint4(s[4 * k], s[4 * k + 1], s[4 * k + 2], s[4 * k + 3]);
+}
+
+__device__ __forceinline__ void load_xyzz(xyzz& p, const xyzz* src)
+{
+    const uint4* q = reinterpret_cast<const uint4*>(src);
+    uint32_t* d = reinterpret_cast<uint32_t*>(&p);
+#pragma unroll
+    for (int k = 0; k < 12; k++) {
+        uint4 v = q[k];
+        d[4 * k] = v.x; d[4 * k + 1] = v.y; d[4 * k + 2] = v.z; d[4 * k + 3] = v.w;
+    }
+}
+
 __device__ __forceinline__ bool aff_is_inf(const affine& a)
 {
     return fp_is_zero_raw(a.x) && fp_is_zero_raw(a.y);

@@ -52,49 +52,6 @@ namespace catmsm {
 
 thread_local LaunchStats g_stats;
 
-// ----------------------------------------------------------------- loads/stores
-__device__ __forceinline__ void load_affine(fp& x, fp& y, const affine* p)
-{
-    const uint4* q = reinterpret_cast<const uint4*>(p);
-    uint4 v[6];
-#pragma unroll
-    for (int k = 0; k < 6; k++) v[k] = __ldg(q + k);
-#pragma unroll
-    for (int k = 0; k < 3; k++) {
-        x.v[4 * k + 0] = v[k].x; x.v[4 * k + 1] = v[k].y;
-        x.v[4 * k + 2] = v[k].z; x.v[4 * k + 3] = v[k].w;
-        y.v[4 * k + 0] = v[k + 3].x; y.v[4 * k + 1] = v[k + 3].y;
-        y.v[4 * k + 2] = v[k + 3].z; y.v[4 * k + 3] = v[k + 3].w;
-    }
-}
-
-__device__ __forceinline__ void store_xyzz(xyzz* dst, const xyzz& p)
-{
-    uint4* q = reinterpret_cast<uint4*>(dst);
-    const uint32_t* s = reinterpret_cast<const uint32_t*>(&p);
-#pragma unroll
-    for (int k = 0; k < 12; k++) q[k] = make_uint4(s[4 * k], s[4 * k + 1], s[4 * k + 2], s[4 * k + 3]);
-}
-
-__device__ __forceinline__ void store_affine(affine* dst, const affine& p)
-{
-    uint4* q = reinterpret_cast<uint4*>(dst);
-    const uint32_t* s = reinterpret_cast<const uint32_t*>(&p);
-#pragma unroll
-    for (int k = 0; k < 6; k++) q[k] = make_uint4(s[4 * k], s[4 * k + 1], s[4 * k + 2], s[4 * k + 3]);
-}
-
-__device__ __forceinline__ void load_xyzz(xyzz& p, const xyzz* src)
-{
-    const uint4* q = reinterpret_cast<const uint4*>(src);
-    uint32_t* d = reinterpret_cast<uint32_t*>(&p);
-#pragma unroll
-    for (int k = 0; k < 12; k++) {
-        uint4 v = q[k];
-        d[4 * k] = v.x; d[4 * k + 1] = v.y; d[4 * k + 2] = v.z; d[4 * k + 3] = v.w;
-    }
-}
-
 // ----------------------------------------------------------------- 1. digits
 // k = the low nbits bits of a little-endian scalar of `stride` bytes
 __device__ __forceinline__ void load_scalar(uint32_t* k, const uint8_t* s, uint32_t stride, uint32_t nbits)
@@ -1032,6 +989,19 @@ static uint32_t accumulate_chunk(size_t nD)
     return best;
 }
 
+// Batch-affine rounds for nD bucket entries over M buckets.  A round pairs
+// entries of one bucket inside one chunk, so it pays only when buckets hold
+// many entries; each round costs three launches per half and one inversion
+// per block.  Measured on GB300 (accumulate stage, ms, rounds 0 / 2 / 3 / 4):
+// 2^20 points 5.38 / 5.03 / 4.89 / 4.93; 2^22 18.45 / 17.48 / 17.10 / 17.15;
+// 2^18 1.43 / 1.51 / 1.61 / 1.72 (fewer entries per bucket: no gain).
+uint32_t msm_affine_rounds(size_t nD, size_t M)
+{
+    const double per = (double)nD / (double)(M ? M : 1);
+    if (nD < (size_t(1) << 24) || per < 16) return 0;
+    return 3;
+}
+
 static bool use_glv(const Ctx* ctx, size_t n, uint32_t nbits)
 {
     return ctx->glv && nbits > 128 && n < (1u << 30);
@@ -1177,8 +1147,14 @@ static cudaError_t msm_run(Ctx* ctx, const void* d_points, const uint8_t* d_scal
         g_stats.launches++;
     }
     mark(4);
-    k_accumulate<<<div_up(chunks, 128), 128, 0, st>>>((const affine*)d_points, sorted_pt, sorted_key, total, L,
-                                                      buckets, head, tail);
+    const uint32_t rounds = tile_window ? 0
+                          : ctx->affine_rounds >= 0 ? (uint32_t)ctx->affine_rounds : msm_affine_rounds(nD, M);
+    if (rounds)
+        CATMSM_CHECK(msm_accumulate_affine(ctx, d_points, sorted_pt, sorted_key, total, L, chunks, rounds, buckets,
+                                           head, tail, st));
+    else
+        k_accumulate<<<div_up(chunks, 128), 128, 0, st>>>((const affine*)d_points, sorted_pt, sorted_key, total, L,
+                                                          buckets, head, tail);
     mark(5);
     if (nD > 2 * (size_t)L * M) {
         // buckets average more than two chunks: tree over each warp's chunks

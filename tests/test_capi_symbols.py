@@ -111,3 +111,23 @@ def test_fft_truncated_prefix_rejects_on_the_host(gpu_binding, oracle):
         ok, out = gpu_binding.p1_fft_truncated_prefix(*args)
         assert not ok and out == jac
 
+
+
+def test_inversion_correction_tables():
+    """fpinv.cuh's KINV_T1[a] = R^3 2^(-32a) mod p and KINV_T2[b] = R 2^(-b)
+    mod p (R = 2^384), recomputed with Python integers."""
+    import re
+    P = 0x1a0111ea397fe69a4b1ba7b6434bacd764774b84f38512bf6730d2a0f6b0f6241eabfffeb153ffffb9feffffffffaaab
+    R = (1 << 384) % P
+    src = open(os.path.join(ROOT, "temp-cat-blst_gb300", "csrc", "fpinv.cuh")).read()
+
+    def table(name):
+        body = src[src.index(name + "["):]          # the declaration, not a comment's mention
+        body = body[body.index("= {") + 3:body.index("};")]
+        rows = re.findall(r"\{([^}]*)\}", body)
+        return [sum(int(w.strip().rstrip("u"), 16) << (32 * i) for i, w in enumerate(r.split(",")) if w.strip())
+                for r in rows]
+    t1, t2 = table("uint32_t KINV_T1"), table("uint32_t KINV_T2")
+    assert len(t1) == 25 and len(t2) == 32
+    assert all(t1[a] == R ** 3 * pow(2, -32 * a, P) % P for a in range(25))
+    assert all(t2[b] == R * pow(2, -b, P) % P for b in range(32))
