@@ -783,7 +783,8 @@ def serving_section(g, synth, torch, dev, rates, seconds):
             row[mode] = {"throughput_req_per_s": len(reqs) / wall,
                          "p50_ms": lat_sorted[len(lat) // 2] if lat else None,
                          "p99_ms": lat_sorted[min(len(lat) - 1, int(0.99 * len(lat)))] if lat else None,
-                         "mean_batch": (st["requests"] / st["batches"]) if st and st["batches"] else 1.0}
+                         "mean_batch": (st["requests"] / st["batches"]) if st and st["batches"] else 1.0,
+                         "max_concurrent_batches": st["max_concurrent"] if st else 1}
         out["rates"].append(row)
         print("serving rate %.1f/s done" % rate, file=sys.stderr, flush=True)
     basis.close()

@@ -352,7 +352,10 @@ void catmsm_server_destroy(void *server);
 int64_t catmsm_server_submit_msm(void *server, const blst_byte *scalars, size_t k);
 int64_t catmsm_server_submit_fft(void *server, blst_p1 *values, size_t n, const blst_fr *domain, int mode);
 int catmsm_server_wait(void *server, int64_t ticket, blst_p1 *msm_out, double *times_ms);
-int catmsm_server_stats(void *server, long *batches, long *batched_requests, long *max_batch);
+/* Engine statistics so far: batches run, requests they held, the largest
+ * batch, and the most batches that were executing at the same time. */
+int catmsm_server_stats(void *server, long *batches, long *batched_requests, long *max_batch,
+                        long *max_concurrent);
 
 /* ---- Batched point decoding and validation (no single reference call; each
  * element has exactly the semantics of the reference call cited):

@@ -132,7 +132,7 @@ def load(build_if_missing=True):
     L.catmsm_server_wait.restype = C.c_int
     L.catmsm_server_wait.argtypes = [_vp, C.c_int64, _vp, _vp]
     L.catmsm_server_stats.restype = C.c_int
-    L.catmsm_server_stats.argtypes = [_vp, _vp, _vp, _vp]
+    L.catmsm_server_stats.argtypes = [_vp, _vp, _vp, _vp, _vp]
     L.catmsm_profile_entries.restype = C.c_double
     L.catmsm_profile_entries.argtypes = []
     L.catmsm_profile_read.restype = C.c_int
@@ -637,6 +637,6 @@ class Server:
         return rc, res, times[0], times[1]
 
     def stats(self):
-        a, b, c = C.c_long(), C.c_long(), C.c_long()
-        self.L.catmsm_server_stats(self.h, C.byref(a), C.byref(b), C.byref(c))
-        return {"batches": a.value, "requests": b.value, "max_batch": c.value}
+        a, b, c, d = C.c_long(), C.c_long(), C.c_long(), C.c_long()
+        self.L.catmsm_server_stats(self.h, C.byref(a), C.byref(b), C.byref(c), C.byref(d))
+        return {"batches": a.value, "requests": b.value, "max_batch": c.value, "max_concurrent": d.value}

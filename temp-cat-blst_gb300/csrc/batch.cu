@@ -428,6 +428,7 @@ cudaError_t batch_run(Basis* b, BatchWork* w, cudaStream_t st, blst_p1* out, uin
 size_t basis_points(const Basis* b) { return b->n; }
 uint32_t basis_window(const Basis* b) { return b->c; }
 int basis_device(const Basis* b) { return b->device; }
+const void* basis_points_device(const Basis* b) { return b->points.p; }
 
 // ---------------------------------------------------------------- autotune cache
 static std::mutex g_tune_mu;

@@ -516,7 +516,9 @@ cudaError_t msm_accumulate_affine(Ctx* ctx, const void* pts, const uint32_t* sor
         !A.prefix || !A.ttot || !A.btot)
         return cudaErrorMemoryAllocation;
     if (!ctx->aff_stream) {
-        CATMSM_CHECK(cudaStreamCreateWithFlags(&ctx->aff_stream, cudaStreamNonBlocking));
+        int prio = 0;
+        CATMSM_CHECK(cudaStreamGetPriority(st, &prio));     // the second half runs at the pipeline stream's priority
+        CATMSM_CHECK(cudaStreamCreateWithPriority(&ctx->aff_stream, cudaStreamNonBlocking, prio));
         CATMSM_CHECK(cudaEventCreateWithFlags(&ctx->aff_fork, cudaEventDisableTiming));
         CATMSM_CHECK(cudaEventCreateWithFlags(&ctx->aff_join, cudaEventDisableTiming));
     }

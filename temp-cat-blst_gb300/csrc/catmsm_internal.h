@@ -26,6 +26,8 @@ cudaError_t batch_run(Basis* b, BatchWork* w, cudaStream_t st, blst_p1* out, uin
 size_t basis_points(const Basis* b);
 uint32_t basis_window(const Basis* b);
 int basis_device(const Basis* b);
+// The basis points (affine, device memory) of the resident basis.
+const void* basis_points_device(const Basis* b);
 
 // Window width, window count and pipeline point count msm_device uses for
 // n points of nbits-bit scalars on this context (2n points of 127 bits when

@@ -7,14 +7,20 @@
 //   FFT  of n Jacobian points with a prepared domain (forward / inverse /
 //        inverse unscaled), in place.
 // W worker threads each own a CUDA stream and a workspace.  Whenever a worker
-// is free it takes the queued requests at the head of the queue as one batch
-// -- every queued MSM, or every queued FFT, up to a point cap -- so requests
-// that arrived while other batches ran join at the next batch boundary, and
-// batches of different workers overlap on the device.  Admission is by HBM
-// budget: a batch starts only while the estimated device memory of all
-// in-flight batches stays within the budget (a single request above the
-// budget runs alone).  Every request records submit/start/done times on the
-// host's steady clock.
+// is free it takes the OLDEST queued request and, as one batch, every other
+// queued request of the same size class (MSMs: k in the same power-of-four
+// band; FFTs: the same n), up to a point cap -- so requests that arrived
+// while other batches ran join at the next batch boundary, a small MSM never
+// waits inside a batch of large ones, and batches of different workers
+// overlap on the device.  Worker 0 runs on the device's highest-priority
+// stream and takes the oldest large request first (see is_large).  MSMs of at
+// least kPlainMinPoints points run through the plain pipeline (GLV split,
+// batch-affine rounds) over the basis points, which beats the fixed-base
+// tables at those sizes; smaller ones run as one batched launch over the
+// tables.  Admission is by HBM budget: a batch starts only while the
+// estimated device memory of all in-flight batches stays within the budget
+// (a single request above the budget runs alone).  Every request records
+// submit/start/done times on the host's steady clock.
 #include "common.cuh"
 #include "catmsm_internal.h"
 #include "catmsm_gpu.h"
@@ -62,6 +68,7 @@ struct Worker {
     Server* s = nullptr;
     std::thread th;
     BatchWork* work = nullptr;
+    int index = 0;
 };
 
 struct Server {
@@ -78,48 +85,105 @@ struct Server {
     std::vector<Worker*> workers;
     // stats
     long batches = 0, batched_reqs = 0, max_batch = 0;
+    long running = 0, max_running = 0;   // batches executing at once
 };
+
+// MSMs of at least this many points take the plain pipeline (msm.cu).
+constexpr size_t kPlainMinPoints = size_t(1) << 18;
+
+// Large requests (FFTs of at least 2^14 points, MSMs of at least 2^20):
+// worker 0 runs on the device's highest-priority stream and takes the oldest
+// large request first, so the longest jobs -- the latency tail -- get SMs
+// ahead of the small batches that share the GPU with them.
+bool is_large(const Request* r) { return r->type == 0 ? r->k >= (size_t(1) << 20) : r->n >= (size_t(1) << 14); }
+
+// Size class: requests of one class are batched together.
+int req_class(const Request* r)
+{
+    size_t x = r->type == 0 ? r->k : r->n;
+    int lg = 0;
+    while (x > 1) {
+        x >>= 1;
+        lg++;
+    }
+    return r->type == 0 ? lg / 2 : 64 + lg;
+}
 
 size_t msm_mem(const Basis* b, size_t k)
 {
+    // the plain pipeline's workspace: ~14 bucket entries per point (GLV halves
+    // over 7-8 windows), each with its index/key/rank words, its slots in the
+    // two batch-affine lists and a share of the prefix products (~240 B)
+    if (k >= kPlainMinPoints) return k * 3400 + ((size_t)64 << 20);
     const size_t D = 256 / basis_window(b) + 1;
     return k * D * 24 + ((size_t)1 << (basis_window(b) - 1)) * 192 * 2 + k * 32 + (1 << 20);
 }
 
 size_t fft_mem(size_t n) { return n * 144 * 2 + n * 64 + (1 << 20); }
 
+// A large MSM through the plain pipeline over the basis points: the scalars
+// are copied to the worker context's device buffer first.
+int run_plain_msm(Server* s, Ctx* ctx, Request* r)
+{
+    uint8_t* d_sc = (uint8_t*)ctx->msm.scalars.get(r->k * 32);
+    if (!d_sc) return (int)cudaErrorMemoryAllocation;
+    cudaError_t err = cudaMemcpyAsync(d_sc, r->scalars, r->k * 32, cudaMemcpyHostToDevice, ctx->stream);
+    uint64_t out[18];
+    if (err == cudaSuccess) err = msm_device(ctx, basis_points_device(s->basis), d_sc, 32, r->k, 256, 0, out);
+    if (err != cudaSuccess) return (int)err;
+    std::memcpy(&r->result, out, sizeof(blst_p1));
+    return 0;
+}
+
 void worker_main(Worker* wk)
 {
     Server* s = wk->s;
     cudaSetDevice(s->device);
     Ctx* ctx = get_ctx();
+    if (ctx && wk->index == 0) {
+        int least = 0, greatest = 0;
+        cudaStream_t ps = nullptr;
+        if (cudaDeviceGetStreamPriorityRange(&least, &greatest) == cudaSuccess &&
+            cudaStreamCreateWithPriority(&ps, cudaStreamNonBlocking, greatest) == cudaSuccess) {
+            cudaStreamSynchronize(ctx->stream);
+            cudaStreamDestroy(ctx->stream);
+            ctx->stream = ps;
+        }
+    }
     for (;;) {
         std::vector<Request*> batch;
         size_t mem = 0;
         {
             std::unique_lock<std::mutex> lk(s->mu);
+            const Request* head = nullptr;
             for (;;) {
                 if (s->stop && s->queue.empty()) return;
+                head = nullptr;
                 if (!s->queue.empty()) {
-                    Request* h = s->queue.front();
-                    const bool fits = s->inflight + h->mem <= s->budget || s->inflight == 0;
+                    head = s->queue.front();
+                    if (wk->index == 0)
+                        for (const Request* r : s->queue)
+                            if (is_large(r)) {
+                                head = r;
+                                break;
+                            }
+                    const bool fits = s->inflight + head->mem <= s->budget || s->inflight == 0;
                     if (fits) break;
                 }
                 s->cv_work.wait(lk);
             }
-            const int type = s->queue.front()->type;
+            const int type = head->type, cls = req_class(head);
+            const size_t cap = type == 0 ? s->msm_cap : s->fft_cap;
             size_t pts = 0;
             for (auto it = s->queue.begin(); it != s->queue.end();) {
                 Request* r = *it;
                 const size_t rp = type == 0 ? r->k : r->n;
-                if (r->type != type) {
+                if (r->type != type || req_class(r) != cls) {
                     ++it;
                     continue;
                 }
                 const bool first = batch.empty();
-                if (!first && (pts + rp > (type == 0 ? s->msm_cap : s->fft_cap) ||
-                               s->inflight + mem + r->mem > s->budget))
-                    break;
+                if (!first && (pts + rp > cap || s->inflight + mem + r->mem > s->budget)) break;
                 batch.push_back(r);
                 pts += rp;
                 mem += r->mem;
@@ -129,12 +193,19 @@ void worker_main(Worker* wk)
             s->batches++;
             s->batched_reqs += (long)batch.size();
             s->max_batch = std::max<long>(s->max_batch, (long)batch.size());
+            s->running++;
+            s->max_running = std::max(s->max_running, s->running);
         }
         const double t0 = now_ms();
         for (Request* r : batch) r->t_start = t0;
         int rc = 0;
         if (!ctx) {
             rc = (int)cudaErrorInitializationError;
+        } else if (batch[0]->type == 0 && batch[0]->k >= kPlainMinPoints) {
+            for (Request* r : batch) {
+                const int e = run_plain_msm(s, ctx, r);
+                if (e && !rc) rc = e;
+            }
         } else if (batch[0]->type == 0) {
             std::vector<size_t> counts(batch.size());
             size_t total = 0;
@@ -169,6 +240,7 @@ void worker_main(Worker* wk)
         {
             std::lock_guard<std::mutex> lk(s->mu);
             s->inflight -= mem;
+            s->running--;
             for (Request* r : batch) {
                 r->status = rc;
                 r->t_done = t1;
@@ -227,6 +299,7 @@ void* catmsm_server_create(void* basis, size_t workers, size_t hbm_budget_bytes)
         delete s;
         return nullptr;
     }
+    for (size_t i = 0; i < s->workers.size(); i++) s->workers[i]->index = (int)i;
     for (Worker* w : s->workers) w->th = std::thread(worker_main, w);
     return s;
 }
@@ -300,7 +373,8 @@ int catmsm_server_wait(void* server, int64_t ticket, blst_p1* msm_out, double* t
     return rc;
 }
 
-int catmsm_server_stats(void* server, long* batches, long* batched_requests, long* max_batch)
+int catmsm_server_stats(void* server, long* batches, long* batched_requests, long* max_batch,
+                        long* max_concurrent)
 {
     Server* s = (Server*)server;
     if (!s) return (int)cudaErrorInvalidValue;
@@ -308,6 +382,7 @@ int catmsm_server_stats(void* server, long* batches, long* batched_requests, lon
     if (batches) *batches = s->batches;
     if (batched_requests) *batched_requests = s->batched_reqs;
     if (max_batch) *max_batch = s->max_batch;
+    if (max_concurrent) *max_concurrent = s->max_running;
     return 0;
 }
 

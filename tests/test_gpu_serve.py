@@ -62,3 +62,45 @@ def test_serving_mix_equals_alone(gpu, oracle, synth):
                 assert oracle.serialize(out[144 * i:144 * i + 144]) == oracle.serialize(alone[144 * i:144 * i + 144])
     server.close()
     basis.close()
+
+
+def test_serving_batches_and_overlaps(gpu, oracle, synth):
+    """Continuous batching is real, not a serial queue: three FFTs of
+    different sizes (three size classes) occupy three workers at once, and
+    a burst of same-class MSMs submitted meanwhile is taken as batches of
+    more than one request; a large MSM (the plain-pipeline route) and the
+    burst results equal the oracle."""
+    n = 1 << 18
+    pts = gpu.points_from_scalars(synth.point_scalars(710, n), n)
+    basis = gpu.Basis(pts, n, 10)
+    server = gpu.Server(basis, workers=3, hbm_budget=4 << 30)
+    ffts = []
+    for e in (12, 13, 14):
+        m = 1 << e
+        jac = oracle.jacobian_randomize(711 + e, m, oracle.gen_points(711 + e, m))
+        dom = gpu.fr_fft_domain_init(m)[1]
+        ffts.append((m, jac, dom, server.submit_fft(jac, m, dom, 0)))
+    burst = []
+    for r in range(64):
+        k = 300 + r
+        sc = synth.scalars(720 + r, k, 0)
+        burst.append((k, sc, server.submit_msm(sc, k)))
+    big_sc = synth.scalars(799, n, 0)
+    big = server.submit_msm(big_sc, n)
+    for m, jac, dom, t in ffts:
+        rc, out, qms, lat = server.wait(t)
+        assert rc == 0
+        ok, alone = gpu.p1_fft_with_domain(jac, m, dom, m + 2, False)
+        assert ok and all(oracle.serialize(out[144 * i:144 * i + 144]) == oracle.serialize(alone[144 * i:144 * i + 144])
+                          for i in range(0, m, 97))
+    for k, sc, t in burst:
+        rc, out, _, _ = server.wait(t)
+        assert rc == 0 and oracle.compress(out) == oracle.msm(pts[:96 * k], sc, k, 256)
+    rc, out, _, _ = server.wait(big)
+    assert rc == 0 and oracle.compress(out) == oracle.compress(gpu.p1s_mult_pippenger(pts, big_sc, n, 256))
+    st = server.stats()
+    assert st["requests"] == 3 + 64 + 1
+    assert st["max_batch"] > 1, st          # requests that queued meanwhile were batched
+    assert st["max_concurrent"] > 1, st     # batches of different workers overlapped
+    server.close()
+    basis.close()
