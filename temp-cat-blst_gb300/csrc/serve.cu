@@ -13,7 +13,8 @@
 // while other batches ran join at the next batch boundary, a small MSM never
 // waits inside a batch of large ones, and batches of different workers
 // overlap on the device.  Worker 0 runs on the device's highest-priority
-// stream and takes the oldest large request first (see is_large).  MSMs of at
+// stream and takes the oldest large request first (see is_large); while a
+// large batch runs, other batches start only after a short hold (kHoldMs).  MSMs of at
 // least kPlainMinPoints points run through the plain pipeline (GLV split,
 // batch-affine rounds) over the basis points, which beats the fixed-base
 // tables at those sizes; smaller ones run as one batched launch over the
@@ -86,7 +87,14 @@ struct Server {
     // stats
     long batches = 0, batched_reqs = 0, max_batch = 0;
     long running = 0, max_running = 0;   // batches executing at once
+    long large_running = 0;              // of those, batches of large requests
 };
+
+// While a large batch runs, another batch starts only once its oldest request
+// has waited this long: at light load a large job (the latency tail) then
+// runs without co-resident work slowing it, and under load the queue still
+// drains concurrently after a bounded delay.
+constexpr double kHoldMs = 10.0;
 
 // MSMs of at least this many points take the plain pipeline (msm.cu).
 constexpr size_t kPlainMinPoints = size_t(1) << 18;
@@ -153,6 +161,7 @@ void worker_main(Worker* wk)
     for (;;) {
         std::vector<Request*> batch;
         size_t mem = 0;
+        bool large = false;
         {
             std::unique_lock<std::mutex> lk(s->mu);
             const Request* head = nullptr;
@@ -168,10 +177,16 @@ void worker_main(Worker* wk)
                                 break;
                             }
                     const bool fits = s->inflight + head->mem <= s->budget || s->inflight == 0;
-                    if (fits) break;
+                    const double waited = now_ms() - head->t_submit;
+                    if (fits && (s->large_running == 0 || waited >= kHoldMs)) break;
+                    if (fits) {
+                        s->cv_work.wait_for(lk, std::chrono::microseconds((long)((kHoldMs - waited) * 1000) + 100));
+                        continue;
+                    }
                 }
                 s->cv_work.wait(lk);
             }
+            large = is_large(head);
             const int type = head->type, cls = req_class(head);
             const size_t cap = type == 0 ? s->msm_cap : s->fft_cap;
             size_t pts = 0;
@@ -195,6 +210,7 @@ void worker_main(Worker* wk)
             s->max_batch = std::max<long>(s->max_batch, (long)batch.size());
             s->running++;
             s->max_running = std::max(s->max_running, s->running);
+            if (large) s->large_running++;
         }
         const double t0 = now_ms();
         for (Request* r : batch) r->t_start = t0;
@@ -241,6 +257,7 @@ void worker_main(Worker* wk)
             std::lock_guard<std::mutex> lk(s->mu);
             s->inflight -= mem;
             s->running--;
+            if (large) s->large_running--;
             for (Request* r : batch) {
                 r->status = rc;
                 r->t_done = t1;
