@@ -518,6 +518,31 @@ int catmsm_fp_inv(blst_fp* out, const blst_fp* a, size_t n)
     return (int)err;
 }
 
+int catmsm_host_fp_inv(blst_fp* out, const blst_fp* a, size_t n)
+{
+    if (n && (!out || !a)) return -1;
+    for (size_t i = 0; i < n; i++) {
+        catmsm_host::hfp x, r;
+        std::memcpy(x.l, &a[i], 48);
+        catmsm_host::inv(r, x);
+        std::memcpy(&out[i], r.l, 48);
+    }
+    return 0;
+}
+
+int catmsm_host_fp_sqr(blst_fp* out, const blst_fp* a, size_t n)
+{
+    if (n && (!out || !a)) return -1;
+    for (size_t i = 0; i < n; i++) {
+        catmsm_host::hfp x, r;
+        std::memcpy(x.l, &a[i], 48);
+        catmsm_host::canon(x);
+        catmsm_host::sqr(r, x);
+        std::memcpy(&out[i], r.l, 48);
+    }
+    return 0;
+}
+
 int catmsm_fp_mul(blst_fp* out, const blst_fp* a, const blst_fp* b, size_t n)
 {
     if (n == 0) return 0;

@@ -111,18 +111,194 @@ inline void sub(hfp& o, const hfp& a, const hfp& b)
     std::memcpy(o.l, t, 48);
 }
 
+// o = a^2 (Montgomery): the 15 cross products once, doubled, plus the 6
+// squares (21 limb products against 36), then the 6 reduction steps.
+inline void sqr(hfp& o, const hfp& a)
+{
+    uint64_t t[13] = {0};
+    for (int i = 0; i < 6; i++) {
+        u128 c = 0;
+        for (int j = i + 1; j < 6; j++) {
+            c += (u128)a.l[i] * a.l[j] + t[i + j];
+            t[i + j] = (uint64_t)c;
+            c >>= 64;
+        }
+        t[i + 6] = (uint64_t)c;
+    }
+    uint64_t top = 0;
+    for (int i = 0; i < 12; i++) {            // double the cross products
+        const uint64_t hi = t[i] >> 63;
+        t[i] = (t[i] << 1) | top;
+        top = hi;
+    }
+    u128 c = 0;
+    for (int i = 0; i < 6; i++) {             // add the squares
+        const u128 sq = (u128)a.l[i] * a.l[i];
+        c += (u128)t[2 * i] + (uint64_t)sq;
+        t[2 * i] = (uint64_t)c;
+        c >>= 64;
+        c += (u128)t[2 * i + 1] + (uint64_t)(sq >> 64);
+        t[2 * i + 1] = (uint64_t)c;
+        c >>= 64;
+    }
+    for (int i = 0; i < 6; i++) {             // Montgomery reduction, one limb at a time
+        const uint64_t m = t[i] * HN0;
+        u128 d = 0;
+        for (int j = 0; j < 6; j++) {
+            d += (u128)m * HP[j] + t[i + j];
+            t[i + j] = (uint64_t)d;
+            d >>= 64;
+        }
+        for (int j = i + 6; j < 13 && d; j++) {
+            d += t[j];
+            t[j] = (uint64_t)d;
+            d >>= 64;
+        }
+    }
+    uint64_t r[6];
+    std::memcpy(r, t + 6, 48);
+    if (t[12] || geq(r, HP)) sub_p(r);
+    std::memcpy(o.l, r, 48);
+}
+
+// R^3 mod p (R = 2^384): a Montgomery multiplication by it maps U^-1 to U^-1 R^2.
+static const uint64_t HR3[6] = {0xed48ac6bd94ca1e0ULL, 0x315f831e03a7adf8ULL, 0x9a53352a615e29ddULL,
+                                0x34c04e5e921e1761ULL, 0x2512d43565724728ULL, 0x0aa6346091755d4dULL};
+
+inline void limbs6_shr(uint64_t* x, unsigned t)
+{
+    while (t >= 64) {
+        for (int i = 0; i < 5; i++) x[i] = x[i + 1];
+        x[5] = 0;
+        t -= 64;
+    }
+    if (t) {
+        for (int i = 0; i < 5; i++) x[i] = (x[i] >> t) | (x[i + 1] << (64 - t));
+        x[5] >>= t;
+    }
+}
+
+inline void limbs6_shl(uint64_t* x, unsigned t)
+{
+    while (t >= 64) {
+        for (int i = 5; i > 0; i--) x[i] = x[i - 1];
+        x[0] = 0;
+        t -= 64;
+    }
+    if (t) {
+        for (int i = 5; i > 0; i--) x[i] = (x[i] << t) | (x[i - 1] >> (64 - t));
+        x[0] <<= t;
+    }
+}
+
+inline uint64_t limbs6_sub(uint64_t* d, const uint64_t* a, const uint64_t* b)
+{
+    uint64_t br = 0;
+    for (int i = 0; i < 6; i++) {
+        const u128 x = (u128)a[i] - b[i] - br;
+        d[i] = (uint64_t)x;
+        br = (uint64_t)(x >> 64) & 1;
+    }
+    return br;
+}
+
+inline void limbs6_add(uint64_t* d, const uint64_t* a, const uint64_t* b)
+{
+    uint64_t c = 0;
+    for (int i = 0; i < 6; i++) {
+        const u128 x = (u128)a[i] + b[i] + c;
+        d[i] = (uint64_t)x;
+        c = (uint64_t)(x >> 64);
+    }
+}
+
+inline unsigned ctz6(const uint64_t* x)
+{
+    unsigned t = 0;
+    for (int i = 0; i < 6; i++) {
+        if (x[i]) return t + (unsigned)__builtin_ctzll(x[i]);
+        t += 64;
+    }
+    return t;
+}
+
+// o = a^-1 in Montgomery form (zero maps to zero), variable time: Kaliski's
+// almost Montgomery inverse (phase 1, every run of trailing zeros in one step)
+// on the Montgomery representation U of a gives X = U^-1 2^k; X 2^-k comes
+// from k / 64 word-wise Montgomery reductions and k % 64 halvings mod p, and
+// one multiplication by R^3 gives U^-1 R^2 = a^-1 R.  ~270 subtract-and-shift
+// steps against ~570 multiplications for a^(p-2).
 inline void inv(hfp& o, const hfp& a)
 {
-    uint64_t e[6];
-    std::memcpy(e, HP, 48);
-    e[0] -= 2;
-    hfp r, b = a;
-    std::memcpy(r.l, HONE, 48);
-    for (int i = 0; i < 381; i++) {
-        if ((e[i / 64] >> (i % 64)) & 1) mul(r, r, b);
-        mul(b, b, b);
+    hfp c = a;
+    canon(c);
+    if (is_zero(c)) {
+        std::memset(o.l, 0, 48);
+        return;
     }
-    o = r;
+    uint64_t u[6], v[6], r[6] = {0}, s[6] = {1, 0, 0, 0, 0, 0}, d[6];
+    std::memcpy(u, HP, 48);
+    std::memcpy(v, c.l, 48);
+    unsigned k = ctz6(v);
+    limbs6_shr(v, k);
+    for (int iter = 0; iter < 2048; iter++) {     // at most ~390 for 381-bit inputs
+        if (limbs6_sub(d, u, v) == 0) {
+            uint64_t z = 0;
+            for (int i = 0; i < 6; i++) z |= d[i];
+            if (z == 0) {                          // u == v == 1
+                limbs6_add(s, r, s);
+                limbs6_shl(r, 1);
+                k += 1;
+                break;
+            }
+            const unsigned t = ctz6(d);            // u > v: u = (u - v) >> t, r += s, s <<= t
+            limbs6_shr(d, t);
+            std::memcpy(u, d, 48);
+            limbs6_add(r, r, s);
+            limbs6_shl(s, t);
+            k += t;
+        } else {
+            limbs6_sub(d, v, u);                   // u < v: v = (v - u) >> t, s += r, r <<= t
+            const unsigned t = ctz6(d);
+            limbs6_shr(d, t);
+            std::memcpy(v, d, 48);
+            limbs6_add(s, r, s);
+            limbs6_shl(r, t);
+            k += t;
+        }
+    }
+    if (geq(r, HP)) sub_p(r);                      // r in (0, 2p): X = p - r
+    hfp X;
+    limbs6_sub(X.l, HP, r);
+    // X 2^-k: whole words by Montgomery reduction steps, the rest by halvings
+    for (; k >= 64; k -= 64) {
+        const uint64_t m = X.l[0] * HN0;
+        u128 acc = ((u128)m * HP[0] + X.l[0]) >> 64;
+        for (int j = 1; j < 6; j++) {
+            acc += (u128)m * HP[j] + X.l[j];
+            X.l[j - 1] = (uint64_t)acc;
+            acc >>= 64;
+        }
+        X.l[5] = (uint64_t)acc;                   // X + m p < 2^448: the quotient fits 6 words, < 2p
+        if (geq(X.l, HP)) sub_p(X.l);
+    }
+    for (; k > 0; k--) {
+        uint64_t top = 0;
+        if (X.l[0] & 1) {
+            uint64_t cy = 0;
+            for (int i = 0; i < 6; i++) {
+                const u128 x = (u128)X.l[i] + HP[i] + cy;
+                X.l[i] = (uint64_t)x;
+                cy = (uint64_t)(x >> 64);
+            }
+            top = cy;
+        }
+        for (int i = 0; i < 5; i++) X.l[i] = (X.l[i] >> 1) | (X.l[i + 1] << 63);
+        X.l[5] = (X.l[5] >> 1) | (top << 63);
+    }
+    hfp r3;
+    std::memcpy(r3.l, HR3, 48);
+    mul(o, X, r3);
 }
 
 inline bool jac_is_inf(const hjac& p) { return is_zero(p.z); }
@@ -132,17 +308,17 @@ inline void jac_dbl(hjac& o, const hjac& p)
 {
     if (jac_is_inf(p)) { o = p; return; }
     hfp A, B, C, D, E, F, t, X3, Y3, Z3;
-    mul(A, p.x, p.x);
-    mul(B, p.y, p.y);
-    mul(C, B, B);
+    sqr(A, p.x);
+    sqr(B, p.y);
+    sqr(C, B);
     add(t, p.x, B);
-    mul(t, t, t);
+    sqr(t, t);
     sub(t, t, A);
     sub(t, t, C);
     add(D, t, t);
     add(E, A, A);
     add(E, E, A);
-    mul(F, E, E);
+    sqr(F, E);
     mul(Z3, p.y, p.z);
     add(Z3, Z3, Z3);
     sub(X3, F, D);
@@ -161,8 +337,8 @@ inline void jac_add(hjac& o, const hjac& a, const hjac& b)
     if (jac_is_inf(a)) { o = b; return; }
     if (jac_is_inf(b)) { o = a; return; }
     hfp z1z1, z2z2, u1, u2, s1, s2, h, r, t;
-    mul(z1z1, a.z, a.z);
-    mul(z2z2, b.z, b.z);
+    sqr(z1z1, a.z);
+    sqr(z2z2, b.z);
     mul(u1, a.x, z2z2);
     mul(u2, b.x, z1z1);
     mul(s1, a.y, b.z);
@@ -177,10 +353,10 @@ inline void jac_add(hjac& o, const hjac& a, const hjac& b)
         return;
     }
     hfp hh, hhh, v, X3, Y3, Z3;
-    mul(hh, h, h);
+    sqr(hh, h);
     mul(hhh, hh, h);
     mul(v, u1, hh);
-    mul(X3, r, r);
+    sqr(X3, r);
     sub(X3, X3, hhh);
     sub(X3, X3, v);
     sub(X3, X3, v);
@@ -215,7 +391,7 @@ inline void normalize(hjac& o, const hjac& p)
     if (jac_is_inf(p)) { std::memset(&o, 0, sizeof(o)); return; }
     hfp zi, zi2, zi3;
     inv(zi, p.z);
-    mul(zi2, zi, zi);
+    sqr(zi2, zi);
     mul(zi3, zi2, zi);
     mul(o.x, p.x, zi2);
     mul(o.y, p.y, zi3);

@@ -891,6 +891,13 @@ uint32_t msm_glv_window(size_t n2)
         const double cost = entries + 4.0 * D * std::ldexp(1.0, (int)c - 1);
         if (bc == 0 || cost < best) { best = cost; bc = c; }
     }
+    // Up to 2^15 points the MSM is latency-bound: a bucket-reduction level is
+    // a chain of dependent additions, so fewer, fuller buckets win over the
+    // work model (measured: 2^13 points c = 8 0.467 ms against c = 10 0.493;
+    // 2^15 points c = 10 0.634 against c = 11 0.677; 2^11 points c = 8 best).
+    uint32_t lg = 0;
+    while ((size_t(2) << lg) <= n2) lg++;
+    if (n2 <= (size_t(1) << 15)) bc = std::min(bc, std::max(8u, lg - 5));
     return bc;
 }
 

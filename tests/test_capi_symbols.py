@@ -80,8 +80,8 @@ def test_msm_plan_heuristics(gpu_binding):
     # n: (window, windows, pipeline points, chunk, level-1 fan-in), GLV on
     expected = {
         1 << 10: (8, 16, 1 << 11, 4, 2),
-        1 << 12: (10, 13, 1 << 13, 6, 2),
-        1 << 14: (11, 12, 1 << 15, 11, 2),
+        1 << 12: (8, 16, 1 << 13, 7, 2),
+        1 << 14: (10, 13, 1 << 15, 11, 2),
         1 << 16: (13, 10, 1 << 17, 34, 2),
         1 << 17: (13, 10, 1 << 18, 45, 2),
         1 << 18: (16, 8, 1 << 19, 54, 8),
@@ -131,3 +131,30 @@ def test_inversion_correction_tables():
     assert len(t1) == 25 and len(t2) == 32
     assert all(t1[a] == R ** 3 * pow(2, -32 * a, P) % P for a in range(25))
     assert all(t2[b] == R * pow(2, -b, P) % P for b in range(32))
+
+
+def test_host_fold_arithmetic(gpu_binding):
+    """The host arithmetic that folds the MSM window sums and normalises the
+    result (no GPU involved): the squaring and the variable-time inversion
+    against Python integers, including 0, 1, p - 1, R and non-canonical
+    inputs in [p, 2^384)."""
+    import random
+    P = 0x1a0111ea397fe69a4b1ba7b6434bacd764774b84f38512bf6730d2a0f6b0f6241eabfffeb153ffffb9feffffffffaaab
+    RM = (1 << 384) % P
+    lib = C.CDLL(gpu_binding.LIB_PATH)
+    rnd = random.Random(21)
+    vals = [0, 1, 2, P - 1, P, P + 1, 2 * P - 1, RM, (1 << 381) - 1, (1 << 384) - 1, 1 << 64, (1 << 64) - 1]
+    vals += [rnd.randrange(1 << 384) for _ in range(3000)]
+    vals += [rnd.randrange(1 << rnd.randrange(1, 381)) for _ in range(1000)]
+    n = len(vals)
+    buf = (C.c_char * (48 * n)).from_buffer(bytearray(b"".join(v.to_bytes(48, "little") for v in vals)))
+    inv_out = (C.c_char * (48 * n))()
+    sqr_out = (C.c_char * (48 * n))()
+    assert lib.catmsm_host_fp_inv(inv_out, buf, C.c_size_t(n)) == 0
+    assert lib.catmsm_host_fp_sqr(sqr_out, buf, C.c_size_t(n)) == 0
+    rinv = pow(RM, -1, P)
+    for i, v in enumerate(vals):
+        a = v % P * rinv % P                    # the field element v represents
+        exp_inv = 0 if a == 0 else pow(a, -1, P) * RM % P
+        assert int.from_bytes(bytes(inv_out[48 * i:48 * i + 48]), "little") == exp_inv, hex(v)
+        assert int.from_bytes(bytes(sqr_out[48 * i:48 * i + 48]), "little") == (v % P) ** 2 * rinv % P, hex(v)
