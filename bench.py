@@ -186,29 +186,29 @@ def dist_setup():
     return ws, rank, local
 
 
-def traffic_from_profile():
-    """DRAM bytes per k_accumulate launch from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "msm_accumulate_ncu.txt")
+def _profile_value(name, key):
+    """A 'key: value' line of a committed ncu summary under profiles/."""
     try:
-        for line in open(path):
-            if line.startswith("dram_bytes_per_launch_full_size:"):
+        for line in open(os.path.join(ROOT, "profiles", name)):
+            if line.startswith(key + ":"):
                 return float(line.split(":", 1)[1].split()[0])
     except OSError:
         pass
     return None
+
+
+def traffic_from_profile(affine):
+    """DRAM bytes of the accumulate stage per MSM at 2^20 from the committed
+    ncu summary: the batch-affine rounds' kernels, or k_accumulate."""
+    if affine:
+        return _profile_value("msm_affine_rounds_n2^20_ncu.txt", "dram_bytes_per_msm_accumulate_stage")
+    return _profile_value("msm_accumulate_ncu.txt", "dram_bytes_per_launch_full_size")
 
 
 def executed_imad_from_profile():
     """Executed fmaheavy-pipe (IMAD) thread instructions per batched-
     commitments batch, from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "batched_commitments_imad.txt")
-    try:
-        for line in open(path):
-            if line.startswith("imad_thread_inst_per_batch:"):
-                return float(line.split(":", 1)[1].split()[0])
-    except OSError:
-        pass
-    return None
+    return _profile_value("batched_commitments_imad.txt", "fmaheavy_inst_per_batch")
 
 
 def run_reference(args, ws, rank):
@@ -334,7 +334,7 @@ def golden():
     return _GOLDEN
 
 
-def batched_section(g, synth, torch, dev, steps, warmup, peak):
+def batched_section(g, synth, torch, dev, steps, warmup, peak, config=None, plain_compare=True):
     """Batched commitments: 1024 commitments per batch over a resident 4096-point
     basis, k_j = floor(2^U), U ~ U[8, 12] (seeded), uniform Fr scalars; the
     batch runs as one CUDA-graph launch with the autotuned (window, chunk);
@@ -352,7 +352,11 @@ def batched_section(g, synth, torch, dev, steps, warmup, peak):
     sc = synth.scalars(seed + 3000, total, 0)
     b = g.Basis(pts, nb)
     t0 = time.perf_counter()
-    window, chunk = b.autotune(counts, sc)
+    if config:
+        b.set_config(*config)
+        window, chunk = config
+    else:
+        window, chunk = b.autotune(counts, sc)
     tune_s = time.perf_counter() - t0
     h_sc = torch.empty(len(sc), dtype=torch.uint8, pin_memory=True)
     h_sc.numpy()[:] = np.frombuffer(sc, dtype=np.uint8)
@@ -368,7 +372,8 @@ def batched_section(g, synth, torch, dev, steps, warmup, peak):
     d_sc = torch.frombuffer(bytearray(sc), dtype=torch.uint8).to(dev)
     torch.cuda.synchronize()
     plain = []
-    for rep in range(2):
+    el = float("nan")
+    for rep in range(2 if plain_compare else 0):
         off = 0
         t = time.perf_counter()
         for j, k in enumerate(counts):
@@ -378,7 +383,8 @@ def batched_section(g, synth, torch, dev, steps, warmup, peak):
             off += k
         el = time.perf_counter() - t
     t_plain = el
-    parity = all(_jac_affine(out[144 * j:144 * j + 144]) == _jac_affine(plain[j]) for j in range(16))
+    parity = all(_jac_affine(out[144 * j:144 * j + 144]) == _jac_affine(plain[j]) for j in range(16)) \
+        if plain_compare else None
     gb = golden().get("batch_commitments")
     gold_ok = None
     if gb and gb["counts"] == counts:
@@ -390,17 +396,22 @@ def batched_section(g, synth, torch, dev, steps, warmup, peak):
     return {"workload": "1024 MSMs/batch, k log-uniform in [256, 4096] over a resident 4096-point basis "
                         "with fixed-base tables, uniform Fr scalars",
             "commits_per_s": nmsm / t_batch, "ms_per_batch": t_batch * 1e3,
-            "plain_commits_per_s": nmsm / t_plain, "speedup_vs_plain": t_plain / t_batch,
+            "plain_commits_per_s": nmsm / t_plain if plain_compare else None,
+            "speedup_vs_plain": t_plain / t_batch if plain_compare else None,
             "points_per_batch": total, "window": window, "chunk": chunk, "autotune_s": tune_s,
             "canonical_timad_s": cm * IMAD_PER_M / t_batch / 1e12,
             "canonical_frac_of_peak": cm * IMAD_PER_M / t_batch / 1e12 / peak if peak > 0 else None,
             "parity_vs_plain_path_first16": parity,
             "parity_vs_reference_golden_all": gold_ok,
-            "executed": ({"imad_per_batch": executed, "fp_mul_equiv_per_batch": executed / IMAD_PER_M,
-                          "timad_s": executed / t_batch / 1e12,
-                          "frac_of_peak": executed / t_batch / 1e12 / peak if peak > 0 else None,
-                          "source": "ncu sm__thread_inst_executed_pipe_fmaheavy_pred_on.sum over the batch's "
-                                    "kernels (profiles/batched_commitments_imad.txt)"} if executed else None),
+            "executed": ({"fmaheavy_inst_per_batch": executed,
+                          "canonical_imad_per_batch": cm * IMAD_PER_M,
+                          "note": "executed = ncu sm__thread_inst_executed_pipe_fmaheavy_pred_on.sum over the batch's "
+                                  "kernels (profiles/batched_commitments_imad.txt): SASS instructions, where a "
+                                  "32x32->64-bit multiply-add is one instruction against two in the canonical "
+                                  "576-IMAD-per-M count (one XYZZ mixed addition: ~2830 instructions against 5760 "
+                                  "canonical); the fixed-base tables skip the per-window reductions and doublings the "
+                                  "canonical count charges, hence canonical_frac_of_peak above 1"}
+                         if executed else None),
             "timing": "host wall clock around each synchronous batch call (H2D of the scalars from pinned "
                       "host memory, one graph launch, D2H of results)"}
 
@@ -816,15 +827,20 @@ def run_ours(args, ws, rank, local):
     synth = _load("catmsm_synth", os.path.join(PKG, "synth.py"))
     g.load()
     n = args.n
+    if args.affine_rounds >= 0:
+        g.msm_affine_rounds(args.affine_rounds)
     dev = torch.device("cuda", local)
     if args.only:
         # one section alone (a diagnostic line, e.g. for an ncu launch list)
         peak = max(g.imad_peak_forms())
         if args.only == "decode":
             out = decode_section(g, synth, torch, dev, args.steps, args.warmup)
+        elif args.only == "batched":
+            cfg = tuple(int(x) for x in args.batched_config.split(",")) if args.batched_config else None
+            out = batched_section(g, synth, torch, dev, args.steps, args.warmup, peak, cfg,
+                                  not args.no_plain_compare)
         else:
-            fn = {"batched": batched_section, "fft": batched_fft_section}[args.only]
-            out = fn(g, synth, torch, dev, args.steps, args.warmup, peak)
+            out = batched_fft_section(g, synth, torch, dev, args.steps, args.warmup, peak)
         print(json.dumps({"section": args.only, args.only: out}))
         return 0
 
@@ -922,6 +938,24 @@ def run_ours(args, ws, rank, local):
 
     acc_ms = stages["accumulate"] / max(calls, 1)
     achieved = entries * MADD_M * IMAD_PER_M / (acc_ms * 1e-3) / 1e12
+    rounds = g.msm_affine_rounds_for(n, NBITS)
+    if rounds > 0:
+        stage_name = ("accumulate stage: %d batch-affine rounds (k_aff_first, k_aff_invert, k_aff_round; two parts "
+                      "on two streams) then the XYZZ fold" % rounds)
+    else:
+        stage_name = "k_accumulate"
+    prof = "msm_affine_rounds_n2^20_ncu.txt"
+    executed = {
+        "fmaheavy_inst_per_msm_stage": _profile_value(prof, "fmaheavy_inst_per_msm_accumulate_stage" if rounds > 0
+                                                      else "fmaheavy_inst_per_msm_xyzz_k_accumulate"),
+        "fmaheavy_inst_per_msm_xyzz_only": _profile_value(prof, "fmaheavy_inst_per_msm_xyzz_k_accumulate"),
+        "fmaheavy_pipe_active_pct_serialised": _profile_value(prof, "fmaheavy_pipe_active_pct_stage_serialised")
+        if rounds > 0 else None,
+        "note": "ncu sm__thread_inst_executed_pipe_fmaheavy_pred_on over the stage's kernels, captured at 2^19 and scaled "
+                "to 2^20 by bucket entries (profiles/%s); SASS instructions, where a 32x32->64-bit multiply-add is one "
+                "instruction against two in the canonical 576-IMAD-per-M count: compare the two counts with each "
+                "other; the canonical frac above charges 10 M per entry, more than batch-affine pairs execute" % prof,
+    } if n == N_POINTS else None
     cm = canonical_m(n)
     canon_tera = cm * IMAD_PER_M / (t_mean * 1e-3) / 1e12
     cpu = None
@@ -953,16 +987,17 @@ def run_ours(args, ws, rank, local):
         "scaling": "weak", "vs_baseline": None, "dtype": "u32",
         "data": "synthetic (seeded: P_i = k_i G, uniform Fr scalars)",
         "config": {"workload": "G1 MSM n=2^20, uniform 255-bit Fr scalars, 96-B affine points",
-                   "n": n, "nbits": NBITS, "window_c": c, "windows": D,
+                   "n": n, "nbits": NBITS, "window_c": c, "windows": D, "affine_rounds": rounds,
                    "glv_split": npipe == 2 * n, "pipeline_points": npipe,
                    "l2": "L2 flushed (256 MB write) between steps; inputs 134 MB + working set > L2",
                    "parallelism": "replicas" if ws > 1 else "single"},
         "e2e": {"value": aggregate_mpoints(ws, n, e2e_ms), "unit": UNIT,
                 "h2d_bytes_per_step": n * 96 + n * 32, "d2h_bytes_per_step": D * 192},
         "gpu_launches": launches,
-        "roofline": {"bound": "imad", "kernel": "k_accumulate", "achieved": achieved, "peak": peak,
+        "roofline": {"bound": "imad", "kernel": stage_name, "achieved": achieved, "peak": peak,
                      "unit": "TIMAD/s", "frac": achieved / peak if peak > 0 else None,
-                     "traffic": traffic_from_profile(),
+                     "traffic": traffic_from_profile(rounds > 0) if n == N_POINTS else None,
+                     "executed": executed,
                      "peak_source": "measured live: max of mad.lo.u32 (%.2f) and mad.wide.u32 (%.2f, 2 per "
                                     "instruction) independent chains on all SMs" % (peak_lo, peak_wide),
                      "work": "%.0f bucket entries x %d M x %d IMAD per launch" % (entries, MADD_M, IMAD_PER_M),
@@ -1019,6 +1054,12 @@ def main():
     ap.add_argument("--n", type=int, default=N_POINTS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--window", type=int, default=0, help="MSM window width (0 = library default)")
+    ap.add_argument("--affine-rounds", type=int, default=-1,
+                    help="batch-affine accumulation rounds (-1 = the library's size rule)")
+    ap.add_argument("--batched-config", default="",
+                    help="with --only batched: window,chunk of the basis instead of autotuning (e.g. 11,96)")
+    ap.add_argument("--no-plain-compare", action="store_true",
+                    help="with --only batched: skip the 1024 plain per-call MSMs it is compared with")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched MSM / FFT sections")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving sweep")
     ap.add_argument("--no-configs", action="store_true",
@@ -1026,7 +1067,7 @@ def main():
     ap.add_argument("--only", choices=["batched", "fft", "decode"], default=None,
                     help="run only the batched-commitments, batched-FFT or decoding section (diagnostic line)")
     ap.add_argument("--serve-rates", default="25,50,100,150", help="Poisson arrival rates (requests/s)")
-    ap.add_argument("--serve-seconds", type=float, default=3.0, help="arrival window per rate")
+    ap.add_argument("--serve-seconds", type=float, default=5.0, help="arrival window per rate")
     args = ap.parse_args()
     ws, rank, local = dist_setup()
     if args.impl == "reference":

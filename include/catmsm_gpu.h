@@ -256,6 +256,9 @@ int catmsm_msm_glv(int enable);
  * -1 = chosen by size (the default).  Returns the previous setting (-2 if no
  * device context); values outside -1..8 only query. */
 int catmsm_msm_affine_rounds(int rounds);
+/* The batch-affine rounds this thread's next MSM of npoints nbits-bit scalars
+ * would run (the setting above, or the size rule); -1 on invalid input. */
+int catmsm_msm_affine_rounds_for(size_t npoints, size_t nbits);
 
 /* Seeded-input support: out[i] = k_i * G (affine, canonical) for n 32-byte
  * little-endian scalars.  Host buffers; returns 0 on success. */

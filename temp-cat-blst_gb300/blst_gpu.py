@@ -93,6 +93,8 @@ def load(build_if_missing=True):
     L.catmsm_msm_glv.argtypes = [C.c_int]
     L.catmsm_msm_affine_rounds.restype = C.c_int
     L.catmsm_msm_affine_rounds.argtypes = [C.c_int]
+    L.catmsm_msm_affine_rounds_for.restype = C.c_int
+    L.catmsm_msm_affine_rounds_for.argtypes = [_sz, _sz]
     L.catmsm_fp_inv.restype = C.c_int
     L.catmsm_fp_inv.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t]
     L.catmsm_p1_affines_from_scalars.restype = C.c_int
@@ -471,6 +473,11 @@ def msm_affine_rounds(rounds: int = -2) -> int:
     """Set (-1 = by size, 0..8) or query (-2) this thread's batch-affine
     accumulation rounds; returns the previous setting."""
     return load().catmsm_msm_affine_rounds(rounds)
+
+
+def msm_affine_rounds_for(n: int, nbits: int = 255) -> int:
+    """Batch-affine rounds this thread's next MSM of n points would run."""
+    return load().catmsm_msm_affine_rounds_for(n, nbits)
 
 
 def fp_inv(a: bytes, n: int) -> bytes:

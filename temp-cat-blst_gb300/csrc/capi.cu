@@ -448,6 +448,17 @@ int catmsm_msm_affine_rounds(int rounds)
     return prev;
 }
 
+int catmsm_msm_affine_rounds_for(size_t npoints, size_t nbits)
+{
+    Ctx* ctx = get_ctx();
+    if (!ctx || npoints == 0 || nbits == 0 || nbits > 256) return -1;
+    uint32_t c, D, chunk, fan_in;
+    size_t pts;
+    msm_plan_detail(npoints, (uint32_t)nbits, ctx->glv, &c, &D, &pts, &chunk, &fan_in);
+    if (ctx->affine_rounds >= 0) return ctx->affine_rounds;
+    return (int)msm_affine_rounds(pts * D, (size_t)D << (c - 1));
+}
+
 int catmsm_msm_plan_detail(size_t npoints, size_t nbits, int glv, size_t* window, size_t* windows, size_t* points,
                            size_t* chunk, size_t* fan_in)
 {
