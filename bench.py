@@ -215,8 +215,10 @@ def run_reference(args, ws, rank):
     """The reference algorithm on the host cores: whole MSM calls of the
     measured workload (the C restatement of the reference's Pippenger,
     oracle/, since the reference tree is not on the GPU host), one call per
-    step, the steps spread over every host thread; value = points of all
-    timed calls / wall time of the timed calls."""
+    step, the steps spread over every host thread; value = the steady-state
+    rate of those threads, threads x points / mean call time (calls past the
+    last full round of threads run with less contention, so this slightly
+    favours the reference over points / wall time)."""
     if rank != 0:
         return 0
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -240,9 +242,9 @@ def run_reference(args, ws, rank):
     if args.warmup:
         run_calls(min(args.warmup, threads))
     wall, per_call, outs = run_calls(args.steps)
-    value = args.steps * n / wall / 1e6
-    parity = all(r.hex() == GOLDEN_2_20 for r in outs) if n == N_POINTS else None
     used = max(1, min(threads, args.steps))
+    value = used * n / statistics.mean(per_call) / 1e6
+    parity = all(r.hex() == GOLDEN_2_20 for r in outs) if n == N_POINTS else None
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": statistics.mean(per_call) * 1e3,
@@ -252,8 +254,10 @@ def run_reference(args, ws, rank):
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": used, "kind": "port",
                          "sample": "%d whole 2^%d-point MSM calls (one per step, window c=%d as the reference "
                                    "picks) of the reference's Pippenger restated in C (oracle/), spread over %d "
-                                   "host threads; %.1f s wall; ms_per_step = mean single-call time"
-                                   % (args.steps, n.bit_length() - 1, ref_window(n), used, wall)},
+                                   "host threads; value = threads x points / mean call time (%.2f Mpoints/s "
+                                   "by points / wall time, %.1f s); ms_per_step = mean single-call time"
+                                   % (args.steps, n.bit_length() - 1, ref_window(n), used,
+                                      args.steps * n / wall / 1e6, wall)},
         "parity_vs_reference_golden": parity,
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
