@@ -181,7 +181,8 @@ __device__ __forceinline__ void fp_mul(fp& r, const fp& a, const fp& b) { r = fp
 // instead of 12: 156 product IMAD instead of 288.  Products of even and odd
 // positions go to the independent E and O accumulators as in fp_mul_impl, and
 // the Montgomery step is the same.  Each step adds at most 4p 2^32, so the
-// running value stays below 6p < 2^384 and the result below 2p.
+// running value stays below 6p < 2^384 and the result below 2p.  The body is
+// the output of gen/gen_fp_sqr.py (in this package), checked by a CPU test.
 __device__ __forceinline__ void fp_sqr_impl(fp& r, const fp& a)
 {
     uint32_t t[12], e[13], o[13], d[12];
