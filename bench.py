@@ -716,7 +716,49 @@ def serving_section(g, synth, torch, dev, rates, seconds):
     build_s = time.perf_counter() - t0
     out = {"workload": "Poisson arrivals; 70%% MSM, k = floor(2^U), U ~ U[10, 22], over a resident 2^22-point "
                        "basis with fixed-base tables (c = 13); 30%% G1 FFT, n = 2^(12..16) uniform; "
-                       "%.0f s per rate" % seconds, "basis_table_build_s": build_s, "rates": []}
+                       "%.0f s per rate; one engine and one plain server for all rates, warmed up first"
+                       % seconds, "basis_table_build_s": build_s, "rates": []}
+
+    def run_plain(r):
+        if r[0] == "msm":
+            g.msm_device(d_pts.data_ptr(), d_pool.data_ptr() + 32 * r[2], 32, r[1], 256)
+        else:
+            ok, _ = g.p1_fft_with_domain(fjac[r[1]], r[1], fdom[r[1]], r[1] + 2, False)
+            assert ok
+
+    # The plain server: one long-lived thread serving requests one at a time
+    # (first come, first served), so its workspaces persist across rates
+    # like the engine's workers'.
+    plain_q, plain_cv = [], threading.Condition()
+
+    def plain_main():
+        while True:
+            with plain_cv:
+                while not plain_q:
+                    plain_cv.wait()
+                item = plain_q.pop(0)
+            if item is None:
+                return
+            item()
+
+    def plain_submit(fn):
+        with plain_cv:
+            plain_q.append(fn)
+            plain_cv.notify()
+
+    plain_th = threading.Thread(target=plain_main, daemon=True)
+    plain_th.start()
+    server = g.Server(basis, workers=4, hbm_budget=48 << 30)
+    # warm-up: the largest requests on every engine worker and on the plain server
+    warm = [("msm", nb, 0)] * 8 + [("fft", fsizes[-1])] * 8 + [("msm", 1 << 12, 0)] * 8
+    tks = [server.submit_msm_ptr(pool_addr, r[1]) if r[0] == "msm" else
+           server.submit_fft(fjac[r[1]], r[1], fdom[r[1]], 0) for r in warm]
+    assert all(server.wait(t)[0] == 0 for t in tks)
+    warm_done = threading.Event()
+    for r in (("msm", nb, 0), ("fft", fsizes[-1]), ("msm", 1 << 12, 0)):
+        plain_submit(lambda r=r: run_plain(r))
+    plain_submit(warm_done.set)
+    warm_done.wait()
     for rate in rates:
         rng = np.random.default_rng(int(rate * 1000))
         arrivals, reqs, t = [], [], 0.0
@@ -734,74 +776,47 @@ def serving_section(g, synth, torch, dev, rates, seconds):
         row = {"rate_per_s": rate, "requests": len(reqs)}
         for mode in ("engine", "plain"):
             lat = [0.0] * len(reqs)
-            server = g.Server(basis, workers=4, hbm_budget=48 << 30) if mode == "engine" else None
-            done = threading.Event()
-            q = []
-            cv = threading.Condition()
+            st0 = server.stats()
+            tickets = []
+            finished = threading.Event()
             start = time.perf_counter()
 
-            def producer():
-                for i, (a, r) in enumerate(zip(arrivals, reqs)):
-                    dt = start + a - time.perf_counter()
-                    if dt > 0:
-                        time.sleep(dt)
-                    ts = time.perf_counter()
-                    if mode == "engine":
-                        if r[0] == "msm":
-                            tk = server.submit_msm_ptr(pool_addr + 32 * r[2], r[1])
-                        else:
-                            tk = server.submit_fft(fjac[r[1]], r[1], fdom[r[1]], 0)
-                        with cv:
-                            q.append((i, ts, tk))
-                            cv.notify()
-                    else:
-                        with cv:
-                            q.append((i, ts, None))
-                            cv.notify()
-                with cv:
-                    q.append(None)
-                    cv.notify()
+            def plain_request(i, ts):
+                run_plain(reqs[i])
+                lat[i] = (time.perf_counter() - ts) * 1e3
 
-            def consumer():
-                while True:
-                    with cv:
-                        while not q:
-                            cv.wait()
-                        item = q.pop(0)
-                    if item is None:
-                        return
-                    i, ts, tk = item
-                    r = reqs[i]
-                    if mode == "engine":
-                        rc, _, _, lat_ms = server.wait(tk)
-                        assert rc == 0
-                        lat[i] = lat_ms                   # submit -> done, measured by the engine
-                        continue
-                    if r[0] == "msm":
-                        g.msm_device(d_pts.data_ptr(), d_pool.data_ptr() + 32 * r[2], 32, r[1], 256)
-                    else:
-                        ok, _ = g.p1_fft_with_domain(fjac[r[1]], r[1], fdom[r[1]], r[1] + 2, False)
-                        assert ok
-                    lat[i] = (time.perf_counter() - ts) * 1e3
-
-            pt = threading.Thread(target=producer)
-            ct = threading.Thread(target=consumer)
-            pt.start()
-            ct.start()
-            pt.join()
-            ct.join()
+            for i, (a, r) in enumerate(zip(arrivals, reqs)):
+                dt = start + a - time.perf_counter()
+                if dt > 0:
+                    time.sleep(dt)
+                ts = time.perf_counter()
+                if mode == "engine":
+                    tickets.append(server.submit_msm_ptr(pool_addr + 32 * r[2], r[1]) if r[0] == "msm" else
+                                   server.submit_fft(fjac[r[1]], r[1], fdom[r[1]], 0))
+                else:
+                    plain_submit(lambda i=i, ts=ts: plain_request(i, ts))
+            if mode == "engine":
+                for i, tk in enumerate(tickets):
+                    rc, _, _, lat_ms = server.wait(tk)
+                    assert rc == 0
+                    lat[i] = lat_ms                       # submit -> done, measured by the engine
+            else:
+                plain_submit(finished.set)
+                finished.wait()
             wall = time.perf_counter() - start
-            st = server.stats() if server else None
-            if server:
-                server.close()
+            st = server.stats()
+            nbt, nrq = st["batches"] - st0["batches"], st["requests"] - st0["requests"]
             lat_sorted = sorted(lat)
             row[mode] = {"throughput_req_per_s": len(reqs) / wall,
                          "p50_ms": lat_sorted[len(lat) // 2] if lat else None,
                          "p99_ms": lat_sorted[min(len(lat) - 1, int(0.99 * len(lat)))] if lat else None,
-                         "mean_batch": (st["requests"] / st["batches"]) if st and st["batches"] else 1.0,
-                         "max_concurrent_batches": st["max_concurrent"] if st else 1}
+                         "mean_batch": (nrq / nbt) if mode == "engine" and nbt else 1.0,
+                         "max_concurrent_batches": st["max_concurrent"] if mode == "engine" else 1}
         out["rates"].append(row)
         print("serving rate %.1f/s done" % rate, file=sys.stderr, flush=True)
+    server.close()
+    plain_submit(None)
+    plain_th.join()
     basis.close()
     return out
 
@@ -839,6 +854,9 @@ def run_ours(args, ws, rank, local):
         peak = max(g.imad_peak_forms())
         if args.only == "decode":
             out = decode_section(g, synth, torch, dev, args.steps, args.warmup)
+        elif args.only == "serving":
+            out = serving_section(g, synth, torch, dev, [float(r) for r in args.serve_rates.split(",")],
+                                  args.serve_seconds)
         elif args.only == "batched":
             cfg = tuple(int(x) for x in args.batched_config.split(",")) if args.batched_config else None
             out = batched_section(g, synth, torch, dev, args.steps, args.warmup, peak, cfg,
@@ -1068,8 +1086,8 @@ def main():
     ap.add_argument("--no-serving", action="store_true", help="skip the serving sweep")
     ap.add_argument("--no-configs", action="store_true",
                     help="skip the plain n=4096 and large-MSM (2^16 / 2^20 / 2^22, all distributions) sections")
-    ap.add_argument("--only", choices=["batched", "fft", "decode"], default=None,
-                    help="run only the batched-commitments, batched-FFT or decoding section (diagnostic line)")
+    ap.add_argument("--only", choices=["batched", "fft", "decode", "serving"], default=None,
+                    help="run only the batched-commitments, batched-FFT, decoding or serving section (diagnostic line)")
     ap.add_argument("--serve-rates", default="25,50,100,150", help="Poisson arrival rates (requests/s)")
     ap.add_argument("--serve-seconds", type=float, default=5.0, help="arrival window per rate")
     args = ap.parse_args()

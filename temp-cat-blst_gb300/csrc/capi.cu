@@ -15,11 +15,56 @@
 #include <new>
 #include <vector>
 
+#include <sys/syscall.h>
+#include <unistd.h>
+
 namespace catmsm {
+
+// Everything a context holds, after its queued work: a worker thread of a
+// short-lived server (or any caller thread) must not leave its workspaces
+// allocated when it exits.
+static void ctx_destroy(Ctx* c)
+{
+    if (cudaSetDevice(c->device) == cudaSuccess) {
+        if (c->stream) cudaStreamSynchronize(c->stream);
+        if (c->copy_stream) cudaStreamSynchronize(c->copy_stream);
+        if (c->aff_stream) cudaStreamSynchronize(c->aff_stream);
+        c->msm.release();
+        c->fft.release();
+        for (PinnedBuf* b : {&c->h_points, &c->h_scalars, &c->h_out, &c->h_values, &c->h_meta}) b->release();
+        for (cudaEvent_t e : c->prof.ev)
+            if (e) cudaEventDestroy(e);
+        for (cudaEvent_t e : {c->points_ready, c->aff_fork, c->aff_join})
+            if (e) cudaEventDestroy(e);
+        for (cudaStream_t st : {c->stream, c->copy_stream, c->aff_stream})
+            if (st) cudaStreamDestroy(st);
+    }
+    delete c;
+}
+
+// The calling thread's contexts, one per device, released at thread exit.
+// The main thread's exit is the process's: its contexts are left to the
+// driver's teardown, so no CUDA call runs while the runtime unloads.
+struct ThreadCtxs {
+    Ctx* per_dev[64] = {nullptr};
+    ~ThreadCtxs()
+    {
+        if ((pid_t)syscall(SYS_gettid) == getpid()) return;
+        int prev = -1;
+        const bool had = cudaGetDevice(&prev) == cudaSuccess;
+        for (Ctx*& c : per_dev)
+            if (c) {
+                ctx_destroy(c);
+                c = nullptr;
+            }
+        if (had) cudaSetDevice(prev);
+    }
+};
 
 Ctx* get_ctx()
 {
-    static thread_local Ctx* per_dev[64] = {nullptr};
+    static thread_local ThreadCtxs ctxs;
+    Ctx** per_dev = ctxs.per_dev;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
     if (!per_dev[dev]) {

@@ -76,6 +76,12 @@ struct PinnedBuf {
         }
         return p;
     }
+    void release()
+    {
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        cap = 0;
+    }
 };
 
 // Device workspaces of one MSM pipeline instance.
@@ -84,10 +90,22 @@ struct MsmWork {
         buckets, head, tail, seg, wins, total, status, misc, glv_pts, glv_sc, glv_sign;
     // batch-affine accumulation rounds (bucket_affine.cu)
     DevBuf aff_pts0, aff_pts1, aff_key0, aff_key1, aff_meta, aff_pairpos, aff_prefix, aff_ttot, aff_btot;
+    void release()
+    {
+        for (DevBuf* b : {&points, &scalars, &digits, &ranks, &counts, &offsets, &block_sums, &sorted_pt,
+                          &sorted_key, &buckets, &head, &tail, &seg, &wins, &total, &status, &misc, &glv_pts,
+                          &glv_sc, &glv_sign, &aff_pts0, &aff_pts1, &aff_key0, &aff_key1, &aff_meta, &aff_pairpos,
+                          &aff_prefix, &aff_ttot, &aff_btot})
+            b->release();
+    }
 };
 
 struct FftWork {
     DevBuf values, roots, glv, scratch, meta;
+    void release()
+    {
+        for (DevBuf* b : {&values, &roots, &glv, &scratch, &meta}) b->release();
+    }
 };
 
 // Per-stage CUDA-event timing of the MSM pipeline (off by default).
@@ -116,7 +134,10 @@ struct Ctx {
     cudaEvent_t aff_fork = nullptr, aff_join = nullptr;
 };
 
-// Per-thread context bound to the thread's current device.
+// Per-thread context bound to the thread's current device.  A thread's
+// contexts (their streams, events and grow-only workspaces: ~15 GB after a
+// 2^22-point MSM) are released when the thread exits; the main thread's are
+// left to process teardown.
 Ctx* get_ctx();
 
 // Launch-time stats, readable through catmsm_last_launches() for the bench.
