@@ -952,9 +952,12 @@ def run_ours(args, ws, rank, local):
         el = time.perf_counter() - t0
         if i >= args.warmup:
             e2e_times.append(el * 1e3)
-    e2e_ms = statistics.mean(e2e_times)
+    # median: the host wall clock also sees rare host-side stalls (one call of ~36 ms among 6.4 ms ones was
+    # observed once); the per-call times and their mean are reported beside it
+    e2e_ms = statistics.median(e2e_times)
+    e2e_mean_ms = statistics.mean(e2e_times)
 
-    t_mean, e2e_ms = max_over_ranks([t_mean, e2e_ms], dist, dev)
+    t_mean, e2e_ms, e2e_mean_ms = max_over_ranks([t_mean, e2e_ms, e2e_mean_ms], dist, dev)
     if rank != 0:
         return 0
 
@@ -1014,7 +1017,11 @@ def run_ours(args, ws, rank, local):
                    "l2": "L2 flushed (256 MB write) between steps; inputs 134 MB + working set > L2",
                    "parallelism": "replicas" if ws > 1 else "single"},
         "e2e": {"value": aggregate_mpoints(ws, n, e2e_ms), "unit": UNIT,
-                "h2d_bytes_per_step": n * 96 + n * 32, "d2h_bytes_per_step": D * 192},
+                "h2d_bytes_per_step": n * 96 + n * 32, "d2h_bytes_per_step": D * 192,
+                "statistic": "median of the timed calls (host wall clock around each synchronous "
+                             "blst_p1s_mult_pippenger call, pinned host buffers)",
+                "mean_value": aggregate_mpoints(ws, n, e2e_mean_ms),
+                "ms_per_call": [round(x, 3) for x in e2e_times]},
         "gpu_launches": launches,
         "roofline": {"bound": "imad", "kernel": stage_name, "achieved": achieved, "peak": peak,
                      "unit": "TIMAD/s", "frac": achieved / peak if peak > 0 else None,
