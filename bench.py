@@ -1096,7 +1096,7 @@ def main():
     ap.add_argument("--only", choices=["batched", "fft", "decode", "serving"], default=None,
                     help="run only the batched-commitments, batched-FFT, decoding or serving section (diagnostic line)")
     ap.add_argument("--serve-rates", default="25,50,100,150", help="Poisson arrival rates (requests/s)")
-    ap.add_argument("--serve-seconds", type=float, default=5.0, help="arrival window per rate")
+    ap.add_argument("--serve-seconds", type=float, default=10.0, help="arrival window per rate")
     args = ap.parse_args()
     ws, rank, local = dist_setup()
     if args.impl == "reference":
