@@ -50,15 +50,18 @@ constexpr int kAffThreads = 128;
 #define CATMSM_AFF_MIN_BLOCKS 4
 #endif
 
-// 48 bytes (one coordinate) from a 16-byte aligned address; Coherent loads
-// go through L2 (data written earlier in the same launch), the others
-// through the read-only path.
-template <bool Coherent>
+// 48 bytes (one coordinate) from a 16-byte aligned address.  Mutable: data
+// this launch may write (a thread's own list slots, prefix products and
+// totals, which only that thread writes and reads back), with plain loads --
+// coherent with the thread's own earlier stores and cached in L1, so the two
+// 16-byte halves of a sector and a thread's consecutive keys hit L1.  The
+// others (read-only for the whole launch) take the read-only path.
+template <bool Mutable>
 __device__ __forceinline__ void load_coord(fp& c, const uint4* q)
 {
 #pragma unroll
     for (int k = 0; k < 3; k++) {
-        const uint4 v = Coherent ? __ldcg(q + k) : __ldg(q + k);
+        const uint4 v = Mutable ? q[k] : __ldg(q + k);
         c.v[4 * k + 0] = v.x; c.v[4 * k + 1] = v.y; c.v[4 * k + 2] = v.z; c.v[4 * k + 3] = v.w;
     }
 }
@@ -72,11 +75,11 @@ __device__ __forceinline__ void stg_fp(fp* dst, const fp& v)
     for (int k = 0; k < 3; k++) q[k] = make_uint4(v.v[4 * k], v.v[4 * k + 1], v.v[4 * k + 2], v.v[4 * k + 3]);
 }
 
-template <bool Coherent>
+template <bool Mutable>
 __device__ __forceinline__ fp ldg_fp(const fp* src)
 {
     fp v;
-    load_coord<Coherent>(v, reinterpret_cast<const uint4*>(src));
+    load_coord<Mutable>(v, reinterpret_cast<const uint4*>(src));
     return v;
 }
 
@@ -89,7 +92,7 @@ struct Row {
 // Items of round 1: sorted entry base + i, a signed point of the GLV array
 // (read-only for the whole accumulation).
 struct SrcSorted {
-    static constexpr bool kCoherent = false;
+    static constexpr bool kMutable = false;
     const affine* pts;
     const uint32_t* sorted_pt;
     const uint32_t* sorted_key;
@@ -103,13 +106,13 @@ struct SrcSorted {
 };
 
 // Items of later rounds: the thread's list, slot base + i.  Its slots may
-// have been written earlier in the same launch, so its loads are coherent.
+// have been written earlier in the same launch (by this thread only).
 struct SrcList {
-    static constexpr bool kCoherent = true;
+    static constexpr bool kMutable = true;
     const affine* pts;
     const uint32_t* keys;
     size_t base;
-    __device__ __forceinline__ uint32_t key(uint32_t i) const { return __ldcg(keys + base + i); }
+    __device__ __forceinline__ uint32_t key(uint32_t i) const { return keys[base + i]; }
     __device__ __forceinline__ Row row(uint32_t i) const
     {
         return Row{reinterpret_cast<const uint4*>(pts + base + i), false};
@@ -119,13 +122,13 @@ struct SrcList {
 template <class Src>
 __device__ __forceinline__ void row_x(const Row& r, fp& x)
 {
-    load_coord<Src::kCoherent>(x, r.p);
+    load_coord<Src::kMutable>(x, r.p);
 }
 
 template <class Src>
 __device__ __forceinline__ void row_y(const Row& r, fp& y)
 {
-    load_coord<Src::kCoherent>(y, r.p + 3);
+    load_coord<Src::kMutable>(y, r.p + 3);
     if (r.neg) fp_neg(y, y);
 }
 
@@ -265,7 +268,7 @@ __device__ __forceinline__ void aff_backward(const Src& src, uint32_t np, affine
         }
         const uint32_t kind = pair_den<Src>(ca, cb, x1, x2, d);
         fp inv;
-        fp_mul(inv, ldg_fp<false>(prefix + pbase + j), I);
+        fp_mul(inv, ldg_fp<true>(prefix + pbase + j), I);   // rewritten by the next forward pass
         fp_mul(I, I, d);
         affine r;
         if (kind == kPairAdd || kind == kPairDbl) {
@@ -416,7 +419,7 @@ __global__ void k_aff_invert(fp* __restrict__ btot, uint32_t nb)
     const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b < nb) {
         fp r;
-        fp_inv_vartime(r, ldg_fp<false>(btot + b));
+        fp_inv_vartime(r, ldg_fp<true>(btot + b));   // overwritten below
         stg_fp(btot + b, r);
     }
 }
@@ -435,8 +438,8 @@ __global__ void __launch_bounds__(kAffThreads, CATMSM_AFF_MIN_BLOCKS) k_aff_roun
     const size_t pbase = (size_t)t * A.H;
     const uint32_t m = A.meta[t];
     const uint32_t np = m & 0xffffu, co = m >> 16;
-    block_product(nd, ldg_fp<false>(A.ttot + t));
-    const fp I = block_leaf_inverse(nd, ldg_fp<false>(A.btot + blk));
+    block_product(nd, ldg_fp<true>(A.ttot + t));                  // both rewritten at the end of this launch
+    const fp I = block_leaf_inverse(nd, ldg_fp<true>(A.btot + blk));
     const uint32_t out = (r - 1) & 1, in = r & 1;
     if (First) {
         const SrcSorted src{A.pts, A.sorted_pt, A.sorted_key, start};
