@@ -105,17 +105,26 @@ struct SrcSorted {
     }
 };
 
-// Items of later rounds: the thread's list, slot base + i.  Its slots may
-// have been written earlier in the same launch (by this thread only).
+// A thread's private arrays (lists, pair positions, prefix products) are
+// slot-major: slot i of thread t is element i T + t (T threads in all), so
+// the lanes of a warp at the same step of their loops touch adjacent
+// elements instead of elements L apart.
+struct Slots {
+    size_t t, T;
+    __device__ __forceinline__ size_t at(uint32_t i) const { return (size_t)i * T + t; }
+};
+
+// Items of later rounds: the thread's list.  Its slots may have been written
+// earlier in the same launch (by this thread only).
 struct SrcList {
     static constexpr bool kMutable = true;
     const affine* pts;
     const uint32_t* keys;
-    size_t base;
-    __device__ __forceinline__ uint32_t key(uint32_t i) const { return keys[base + i]; }
+    Slots sl;
+    __device__ __forceinline__ uint32_t key(uint32_t i) const { return keys[sl.at(i)]; }
     __device__ __forceinline__ Row row(uint32_t i) const
     {
-        return Row{reinterpret_cast<const uint4*>(pts + base + i), false};
+        return Row{reinterpret_cast<const uint4*>(pts + sl.at(i)), false};
     }
 };
 
@@ -180,8 +189,8 @@ __device__ __forceinline__ void copy_item(const Src& src, uint32_t i, affine* ds
 // Returns the product of all denominators; *np_out = pairs, *cnt_out = items
 // of the output list.
 template <class Src>
-__device__ __forceinline__ fp aff_forward(const Src& src, uint32_t cnt, affine* outP, uint32_t* outK, size_t obase,
-                                          uint32_t* pairpos, fp* prefix, size_t pbase, uint32_t* np_out,
+__device__ __forceinline__ fp aff_forward(const Src& src, uint32_t cnt, affine* outP, uint32_t* outK, Slots os,
+                                          uint32_t* pairpos, fp* prefix, Slots ps, uint32_t* np_out,
                                           uint32_t* cnt_out)
 {
     uint32_t o = 0, np = 0, pi = 0, pk = 0;
@@ -195,15 +204,15 @@ __device__ __forceinline__ fp aff_forward(const Src& src, uint32_t cnt, affine* 
             const uint32_t i = i0 + u;
             if (i < cnt) {
                 if (pend && kk[u] == pk) {
-                    pairpos[pbase + np] = (pi << 16) | o;
-                    outK[obase + o] = pk;
+                    pairpos[ps.at(np)] = (pi << 16) | o;
+                    outK[os.at(o)] = pk;
                     np++;
                     o++;
                     pend = false;
                 } else {
                     if (pend) {
-                        copy_item(src, pi, outP + obase + o);
-                        outK[obase + o] = pk;
+                        copy_item(src, pi, outP + os.at(o));
+                        outK[os.at(o)] = pk;
                         o++;
                     }
                     pend = true;
@@ -214,8 +223,8 @@ __device__ __forceinline__ fp aff_forward(const Src& src, uint32_t cnt, affine* 
         }
     }
     if (pend) {
-        copy_item(src, pi, outP + obase + o);
-        outK[obase + o] = pk;
+        copy_item(src, pi, outP + os.at(o));
+        outK[os.at(o)] = pk;
         o++;
     }
     *np_out = np;
@@ -223,7 +232,7 @@ __device__ __forceinline__ fp aff_forward(const Src& src, uint32_t cnt, affine* 
     fp q;
     fp_set_one(q);
     if (np == 0) return q;
-    uint32_t ip = pairpos[pbase] >> 16;
+    uint32_t ip = pairpos[ps.at(0)] >> 16;
     Row ra = src.row(ip), rb = src.row(ip + 1);
     for (uint32_t j = 0; j < np; j++) {
         fp x1, x2, d;
@@ -231,12 +240,12 @@ __device__ __forceinline__ fp aff_forward(const Src& src, uint32_t cnt, affine* 
         row_x<Src>(rb, x2);
         const Row ca = ra, cb = rb;
         if (j + 1 < np) {
-            ip = pairpos[pbase + j + 1] >> 16;
+            ip = pairpos[ps.at(j + 1)] >> 16;
             ra = src.row(ip);
             rb = src.row(ip + 1);
         }
         pair_den<Src>(ca, cb, x1, x2, d);
-        stg_fp(prefix + pbase + j, q);
+        stg_fp(prefix + ps.at(j), q);
         fp_mul(q, q, d);
     }
     return q;
@@ -247,11 +256,11 @@ __device__ __forceinline__ fp aff_forward(const Src& src, uint32_t cnt, affine* 
 // its output slot.  The previous pair's rows are fetched before this pair's
 // arithmetic.
 template <class Src>
-__device__ __forceinline__ void aff_backward(const Src& src, uint32_t np, affine* outP, size_t obase,
-                                             const uint32_t* pairpos, const fp* prefix, size_t pbase, fp I)
+__device__ __forceinline__ void aff_backward(const Src& src, uint32_t np, affine* outP, Slots os,
+                                             const uint32_t* pairpos, const fp* prefix, Slots ps, fp I)
 {
     if (np == 0) return;
-    uint32_t pp = pairpos[pbase + np - 1];
+    uint32_t pp = pairpos[ps.at(np - 1)];
     Row ra = src.row(pp >> 16), rb = src.row((pp >> 16) + 1);
     for (uint32_t j = np; j-- > 0;) {
         fp x1, y1, x2, y2, d;
@@ -262,13 +271,13 @@ __device__ __forceinline__ void aff_backward(const Src& src, uint32_t np, affine
         const Row ca = ra, cb = rb;
         const uint32_t o = pp & 0xffffu;
         if (j > 0) {
-            pp = pairpos[pbase + j - 1];
+            pp = pairpos[ps.at(j - 1)];
             ra = src.row(pp >> 16);
             rb = src.row((pp >> 16) + 1);
         }
         const uint32_t kind = pair_den<Src>(ca, cb, x1, x2, d);
         fp inv;
-        fp_mul(inv, ldg_fp<true>(prefix + pbase + j), I);   // rewritten by the next forward pass
+        fp_mul(inv, ldg_fp<true>(prefix + ps.at(j)), I);   // rewritten by the next forward pass
         fp_mul(I, I, d);
         affine r;
         if (kind == kPairAdd || kind == kPairDbl) {
@@ -297,7 +306,7 @@ __device__ __forceinline__ void aff_backward(const Src& src, uint32_t np, affine
             fp_zero(r.x);
             fp_zero(r.y);
         }
-        store_affine(outP + obase + o, r);
+        store_affine(outP + os.at(o), r);
     }
 }
 
@@ -380,11 +389,12 @@ struct AffArgs {
     const uint32_t* sorted_key;
     const uint32_t* total_ptr;    // E, the number of sorted entries
     uint32_t L, H;                // chunk length, pair slots per thread (ceil(L / 2))
-    affine* list_pts[2];          // per-thread lists: slot t L + i
+    size_t T;                     // threads of the whole grid (both halves): the slot-major stride
+    affine* list_pts[2];          // per-thread lists: slot i of thread t at i T + t
     uint32_t* list_key[2];
     uint32_t* meta;               // per thread: pairs | output items << 16 of the round in flight
-    uint32_t* pairpos;            // t H + j: input position << 16 | output slot
-    fp* prefix;                   // t H + j: product of the denominators of pairs after j
+    uint32_t* pairpos;            // pair j of thread t at j T + t: input position << 16 | output slot
+    fp* prefix;                   // pair j of thread t at j T + t: its prefix product
     fp* ttot;                     // per thread: product of its denominators
     fp* btot;                     // per block: product of its threads' products, then its inverse
     xyzz* buckets;
@@ -404,8 +414,8 @@ __global__ void __launch_bounds__(kAffThreads, CATMSM_AFF_MIN_BLOCKS) k_aff_firs
     const uint32_t cnt = start < E ? (uint32_t)min((size_t)A.L, (size_t)E - start) : 0;
     const SrcSorted src{A.pts, A.sorted_pt, A.sorted_key, start};
     uint32_t np = 0, co = 0;
-    const fp tot = aff_forward(src, cnt, A.list_pts[0], A.list_key[0], start, A.pairpos, A.prefix,
-                               (size_t)t * A.H, &np, &co);
+    const Slots sl{t, A.T};
+    const fp tot = aff_forward(src, cnt, A.list_pts[0], A.list_key[0], sl, A.pairpos, A.prefix, sl, &np, &co);
     A.meta[t] = np | (co << 16);
     stg_fp(A.ttot + t, tot);
     const fp root = block_product(nd, tot);
@@ -435,7 +445,7 @@ __global__ void __launch_bounds__(kAffThreads, CATMSM_AFF_MIN_BLOCKS) k_aff_roun
     const uint32_t t = blk * blockDim.x + threadIdx.x;
     const uint32_t E = *A.total_ptr;
     const size_t start = (size_t)t * A.L;
-    const size_t pbase = (size_t)t * A.H;
+    const Slots sl{t, A.T};
     const uint32_t m = A.meta[t];
     const uint32_t np = m & 0xffffu, co = m >> 16;
     block_product(nd, ldg_fp<true>(A.ttot + t));                  // both rewritten at the end of this launch
@@ -443,18 +453,18 @@ __global__ void __launch_bounds__(kAffThreads, CATMSM_AFF_MIN_BLOCKS) k_aff_roun
     const uint32_t out = (r - 1) & 1, in = r & 1;
     if (First) {
         const SrcSorted src{A.pts, A.sorted_pt, A.sorted_key, start};
-        aff_backward(src, np, A.list_pts[out], start, A.pairpos, A.prefix, pbase, I);
+        aff_backward(src, np, A.list_pts[out], sl, A.pairpos, A.prefix, sl, I);
     } else {
-        const SrcList src{A.list_pts[in], A.list_key[in], start};
-        aff_backward(src, np, A.list_pts[out], start, A.pairpos, A.prefix, pbase, I);
+        const SrcList src{A.list_pts[in], A.list_key[in], sl};
+        aff_backward(src, np, A.list_pts[out], sl, A.pairpos, A.prefix, sl, I);
     }
-    const SrcList list{A.list_pts[out], A.list_key[out], start};
+    const SrcList list{A.list_pts[out], A.list_key[out], sl};
     if (Last) {
         aff_fold(list, co, A.sorted_key, start, E, A.L, t, A.buckets, A.head, A.tail);
     } else {
         uint32_t np2 = 0, co2 = 0;
-        const fp tot = aff_forward(list, co, A.list_pts[in], A.list_key[in], start, A.pairpos, A.prefix, pbase,
-                                   &np2, &co2);
+        const fp tot = aff_forward(list, co, A.list_pts[in], A.list_key[in], sl, A.pairpos, A.prefix, sl, &np2,
+                                   &co2);
         A.meta[t] = np2 | (co2 << 16);
         stg_fp(A.ttot + t, tot);
         __syncthreads();                      // every leaf inverse of this round is read
@@ -503,6 +513,7 @@ cudaError_t msm_accumulate_affine(Ctx* ctx, const void* pts, const uint32_t* sor
     A.total_ptr = total;
     A.L = L;
     A.H = H;
+    A.T = threads;
     A.list_pts[0] = (affine*)W.aff_pts0.get(threads * L * sizeof(affine));
     A.list_pts[1] = (affine*)W.aff_pts1.get(threads * L * sizeof(affine));
     A.list_key[0] = (uint32_t*)W.aff_key0.get(threads * L * 4);
