@@ -15,10 +15,10 @@
 // overlap on the device.  Worker 0 runs on the device's highest-priority
 // stream and takes the oldest large request first (see is_large); while a
 // large batch runs, other batches start only after a short hold (kHoldMs).  MSMs of at
-// least kPlainMinPoints points run through the plain pipeline (GLV split,
-// batch-affine rounds) over the basis points, which beats the fixed-base
-// tables at those sizes; smaller ones run as one batched launch over the
-// tables.  Admission is by HBM budget: a batch starts only while the
+// least kPlainMinPoints points, and a batch of a single MSM, run through the
+// plain pipeline (GLV split, batch-affine rounds) over the basis points,
+// which beats the fixed-base tables there; batches of several smaller ones
+// run as one batched launch over the tables.  Admission is by HBM budget: a batch starts only while the
 // estimated device memory of all in-flight batches stays within the budget
 // (a single request above the budget runs alone).  Every request records
 // submit/start/done times on the host's steady clock.
@@ -96,7 +96,11 @@ struct Server {
 // drains concurrently after a bounded delay.
 constexpr double kHoldMs = 10.0;
 
-// MSMs of at least this many points take the plain pipeline (msm.cu).
+// MSMs of at least this many points take the plain pipeline (msm.cu), and
+// so does a batch of one MSM of any size: for a lone request the fixed-base
+// tables' batched launch sequence is slower (measured on the 2^22-point basis,
+// c = 13: 2^12 points 0.66 against 0.44 ms, 2^16 1.61 against 0.98, 2^17 2.58
+// against 1.51); the tables win once several MSMs share one batch.
 constexpr size_t kPlainMinPoints = size_t(1) << 18;
 
 // Large requests (FFTs of at least 2^14 points, MSMs of at least 2^20):
@@ -122,9 +126,13 @@ size_t msm_mem(const Basis* b, size_t k)
     // the plain pipeline's workspace: ~14 bucket entries per point (GLV halves
     // over 7-8 windows), each with its index/key/rank words, its slots in the
     // two batch-affine lists and a share of the prefix products (~240 B)
-    if (k >= kPlainMinPoints) return k * 3400 + ((size_t)64 << 20);
+    const size_t plain = k * 3400 + ((size_t)64 << 20);
+    if (k >= kPlainMinPoints) return plain;
+    // a smaller MSM runs over the tables in a batch, or through the plain
+    // pipeline alone: the larger of the two
     const size_t D = 256 / basis_window(b) + 1;
-    return k * D * 24 + ((size_t)1 << (basis_window(b) - 1)) * 192 * 2 + k * 32 + (1 << 20);
+    const size_t table = k * D * 24 + ((size_t)1 << (basis_window(b) - 1)) * 192 * 2 + k * 32 + (1 << 20);
+    return std::max(plain, table);
 }
 
 size_t fft_mem(size_t n) { return n * 144 * 2 + n * 64 + (1 << 20); }
@@ -217,7 +225,7 @@ void worker_main(Worker* wk)
         int rc = 0;
         if (!ctx) {
             rc = (int)cudaErrorInitializationError;
-        } else if (batch[0]->type == 0 && batch[0]->k >= kPlainMinPoints) {
+        } else if (batch[0]->type == 0 && (batch[0]->k >= kPlainMinPoints || batch.size() == 1)) {
             for (Request* r : batch) {
                 const int e = run_plain_msm(s, ctx, r);
                 if (e && !rc) rc = e;
