@@ -704,10 +704,11 @@ def serving_section(g, synth, torch, dev, rates, seconds):
     assert g.load().catmsm_p1_affines_from_scalars_device(d_pts.data_ptr(), k_pts.data_ptr(), nb) == 0
     del k_pts
     pts = bytes(d_pts.cpu().numpy())
-    import ctypes
-    pool = bytearray(synth.scalars(5005, nb, 0))        # scalars of a request: a slice of the pool
-    pool_addr = ctypes.addressof((ctypes.c_char * len(pool)).from_buffer(pool))
-    d_pool = torch.frombuffer(pool, dtype=torch.uint8).to(dev)
+    # scalars of a request: a slice of the pool, in pinned host memory (a server receives requests into
+    # pinned buffers; the engine copies each request's scalars to the device, the plain server reads d_pool)
+    pool = torch.frombuffer(bytearray(synth.scalars(5005, nb, 0)), dtype=torch.uint8).pin_memory()
+    pool_addr = pool.data_ptr()
+    d_pool = pool.to(dev)
     fsizes = [1 << e for e in range(12, 17)]
     fjac = {n: _jacobian_z1(pts, n) for n in fsizes}
     fdom = {n: g.fr_fft_domain_init(n)[1] for n in fsizes}
