@@ -18,8 +18,10 @@
 // item passes through; the results form the thread's list for the next
 // round, still in bucket order.  Round 1 reads the sorted entries (a gather
 // of signed points); later rounds read the list the previous round wrote.
+// A thread's lists, pair positions and prefix products are slot-major (see
+// Slots), so a warp's accesses at one step of the loops are adjacent.
 // One round is three launches:
-//   forward   each thread walks its pairs from last to first, storing the
+//   forward   each thread walks its pairs from first to last, storing the
 //             running product of the denominators before each pair (its
 //             prefix) and ending with its total; the block multiplies its
 //             threads' totals in a shared-memory tree;
@@ -27,7 +29,7 @@
 //             (fp_inv_vartime: tens of microseconds, not Fermat's ~0.45 ms);
 //   backward  the block re-forms the tree, pushes the inverse down to a
 //             per-thread inverse of its total, and each thread walks its
-//             pairs from first to last: inv(d_j) = prefix_j * I, I *= d_j,
+//             pairs from last to first: inv(d_j) = prefix_j * I, I *= d_j,
 //             then the affine sum.  The same kernel then runs the next
 //             round's forward pass, or, after the last round, folds the
 //             remaining list into the chunk's bucket / head / tail exactly as
