@@ -121,7 +121,7 @@ class Clocks:
 
 
 class NvmlClocks:
-    """SM clock and clock-event reasons read through NVML (the driver's
+    """SM clock and clock-event reasons read through NVML (libnvidia-ml's
     libnvidia-ml, via ctypes) every ~2 ms on a background thread during the
     timed region; read-only.  Falls back to the nvidia-smi sampler when NVML
     cannot be opened."""

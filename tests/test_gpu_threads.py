@@ -67,7 +67,7 @@ def test_concurrent_calls_from_threads(gpu, oracle, synth):
             assert results[i] == exp, (kind, n)
 
 
-SLACK = 96 << 20   # device-wide free memory may move by a few MB (other allocations, the driver)
+SLACK = 96 << 20   # device-wide free memory may move by a few MB (other allocations, the CUDA runtime)
 
 
 def _free():
