@@ -121,8 +121,8 @@ class Clocks:
 
 
 class NvmlClocks:
-    """SM clock and clock-event reasons read through NVML (libnvidia-ml's
-    libnvidia-ml, via ctypes) every ~2 ms on a background thread during the
+    """SM clock and clock-event reasons read through NVML (libnvidia-ml,
+    via ctypes) every ~2 ms on a background thread during the
     timed region; read-only.  Falls back to the nvidia-smi sampler when NVML
     cannot be opened."""
     REASONS = ((0x4, "sw_power_cap"), (0x8, "hw_slowdown"), (0x20, "sw_thermal_slowdown"),
