@@ -31,6 +31,16 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 PKG = os.path.join(ROOT, "temp-cat-blst_gb300")
 
 METRIC = "G1 MSM Mpoints/s at n=2^20"
+
+
+def size_name(n):
+    """n as 2^k when it is a power of two."""
+    return "2^%d" % (n.bit_length() - 1) if n > 0 and n & (n - 1) == 0 else str(n)
+
+
+def metric_name(n):
+    """The metric line's name for an MSM of n points (METRIC at the default n)."""
+    return "G1 MSM Mpoints/s at n=" + size_name(n)
 UNIT = "Mpoints/s"
 N_POINTS = 1 << 20
 NBITS = 255
@@ -246,11 +256,11 @@ def run_reference(args, ws, rank):
     value = used * n / statistics.mean(per_call) / 1e6
     parity = all(r.hex() == GOLDEN_2_20 for r in outs) if n == N_POINTS else None
     line = {
-        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
+        "impl": "reference", "metric": metric_name(n), "value": value, "unit": UNIT, "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": statistics.mean(per_call) * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
         "data": "synthetic (seeded)",
-        "config": {"workload": "G1 MSM n=2^20, uniform 255-bit Fr scalars", "n": n, "nbits": NBITS},
+        "config": {"workload": "G1 MSM n=%s, uniform 255-bit Fr scalars" % size_name(n), "n": n, "nbits": NBITS},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": used, "kind": "port",
                          "sample": "%d whole 2^%d-point MSM calls (one per step, window c=%d as the reference "
                                    "picks) of the reference's Pippenger restated in C (oracle/), spread over %d "
@@ -1008,14 +1018,15 @@ def run_ours(args, ws, rank, local):
         serving = serving_section(g, synth, torch, dev, [float(r) for r in args.serve_rates.split(",")],
                                   args.serve_seconds)
     line = {
-        "metric": METRIC, "value": aggregate_mpoints(ws, n, t_mean), "unit": UNIT, "n_gpus": ws,
+        "metric": metric_name(n), "value": aggregate_mpoints(ws, n, t_mean), "unit": UNIT, "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_mean, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u32",
         "data": "synthetic (seeded: P_i = k_i G, uniform Fr scalars)",
-        "config": {"workload": "G1 MSM n=2^20, uniform 255-bit Fr scalars, 96-B affine points",
+        "config": {"workload": "G1 MSM n=%s, uniform 255-bit Fr scalars, 96-B affine points" % size_name(n),
                    "n": n, "nbits": NBITS, "window_c": c, "windows": D, "affine_rounds": rounds,
                    "glv_split": npipe == 2 * n, "pipeline_points": npipe,
-                   "l2": "L2 flushed (256 MB write) between steps; inputs 134 MB + working set > L2",
+                   "l2": "L2 flushed (256 MB write) between steps; inputs %d MB + working set > L2"
+                         % round(n * 128 / 1e6),
                    "parallelism": "replicas" if ws > 1 else "single"},
         "e2e": {"value": aggregate_mpoints(ws, n, e2e_ms), "unit": UNIT,
                 "h2d_bytes_per_step": n * 96 + n * 32, "d2h_bytes_per_step": D * 192,
