@@ -385,10 +385,11 @@ int catmsm_fp_mul(blst_fp *out, const blst_fp *a, const blst_fp *b, size_t n);
  * blst_fp with inputs below 2p.  Returns 0 on success. */
 int catmsm_fp_inv(blst_fp *out, const blst_fp *a, size_t n);
 /* Self-checks of the host arithmetic that folds the MSM window sums (no GPU
- * needed): out[i] = a[i]^-1 and a[i]^2, Montgomery form, canonical outputs,
- * inputs below 2^384 (reduced first).  Return 0. */
+ * needed): out[i] = a[i]^-1, a[i]^2 and a[i] b[i], Montgomery form, canonical
+ * outputs, inputs below 2^384 (reduced first).  Return 0. */
 int catmsm_host_fp_inv(blst_fp *out, const blst_fp *a, size_t n);
 int catmsm_host_fp_sqr(blst_fp *out, const blst_fp *a, size_t n);
+int catmsm_host_fp_mul(blst_fp *out, const blst_fp *a, const blst_fp *b, size_t n);
 
 #ifdef __cplusplus
 }

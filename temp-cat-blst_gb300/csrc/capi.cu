@@ -599,6 +599,21 @@ int catmsm_host_fp_sqr(blst_fp* out, const blst_fp* a, size_t n)
     return 0;
 }
 
+int catmsm_host_fp_mul(blst_fp* out, const blst_fp* a, const blst_fp* b, size_t n)
+{
+    if (n && (!out || !a || !b)) return -1;
+    for (size_t i = 0; i < n; i++) {
+        catmsm_host::hfp x, y, r;
+        std::memcpy(x.l, &a[i], 48);
+        std::memcpy(y.l, &b[i], 48);
+        catmsm_host::canon(x);
+        catmsm_host::canon(y);
+        catmsm_host::mul(r, x, y);
+        std::memcpy(&out[i], r.l, 48);
+    }
+    return 0;
+}
+
 int catmsm_fp_mul(blst_fp* out, const blst_fp* a, const blst_fp* b, size_t n)
 {
     if (n == 0) return 0;

@@ -50,31 +50,35 @@ inline bool is_zero(const hfp& a)
     return z == 0;
 }
 
+// o = a b R^-1 mod p for canonical a, b (CIOS, the multiplication and the
+// reduction of each word of b in one pass).  With a, b < p the running value
+// t stays below 2p < 2^382, so the carry chains of the products (A) and of
+// the reduction (C) meet in t[5] without overflow and no carry words beyond
+// six are needed.  Measured on the Grace host: 43 ns against 51 for separate
+// multiply and reduce passes, and 41 ns as the squaring against 51 for a
+// dedicated squaring (the halved cross products do not pay at 6 words).
 inline void mul(hfp& o, const hfp& a, const hfp& b)
 {
-    uint64_t t[8] = {0};
+    uint64_t t[6] = {0, 0, 0, 0, 0, 0};
+#pragma GCC unroll 6
     for (int i = 0; i < 6; i++) {
-        u128 c = 0;
-        for (int j = 0; j < 6; j++) {
-            c += (u128)a.l[j] * b.l[i] + t[j];
-            t[j] = (uint64_t)c;
-            c >>= 64;
-        }
-        c += t[6];
-        t[6] = (uint64_t)c;
-        t[7] = (uint64_t)(c >> 64);
-        uint64_t m = t[0] * HN0;
-        c = ((u128)m * HP[0] + t[0]) >> 64;
+        const uint64_t bi = b.l[i];
+        u128 c = (u128)a.l[0] * bi + t[0];
+        uint64_t A = (uint64_t)(c >> 64);
+        const uint64_t t0 = (uint64_t)c;
+        const uint64_t m = t0 * HN0;
+        uint64_t C = (uint64_t)(((u128)m * HP[0] + t0) >> 64);
+#pragma GCC unroll 5
         for (int j = 1; j < 6; j++) {
-            c += (u128)m * HP[j] + t[j];
-            t[j - 1] = (uint64_t)c;
-            c >>= 64;
+            c = (u128)a.l[j] * bi + t[j] + A;
+            A = (uint64_t)(c >> 64);
+            const u128 d = (u128)m * HP[j] + (uint64_t)c + C;
+            t[j - 1] = (uint64_t)d;
+            C = (uint64_t)(d >> 64);
         }
-        c += t[6];
-        t[5] = (uint64_t)c;
-        t[6] = t[7] + (uint64_t)(c >> 64);
+        t[5] = C + A;
     }
-    if (t[6] || geq(t, HP)) sub_p(t);
+    if (geq(t, HP)) sub_p(t);
     std::memcpy(o.l, t, 48);
 }
 
@@ -111,55 +115,8 @@ inline void sub(hfp& o, const hfp& a, const hfp& b)
     std::memcpy(o.l, t, 48);
 }
 
-// o = a^2 (Montgomery): the 15 cross products once, doubled, plus the 6
-// squares (21 limb products against 36), then the 6 reduction steps.
-inline void sqr(hfp& o, const hfp& a)
-{
-    uint64_t t[13] = {0};
-    for (int i = 0; i < 6; i++) {
-        u128 c = 0;
-        for (int j = i + 1; j < 6; j++) {
-            c += (u128)a.l[i] * a.l[j] + t[i + j];
-            t[i + j] = (uint64_t)c;
-            c >>= 64;
-        }
-        t[i + 6] = (uint64_t)c;
-    }
-    uint64_t top = 0;
-    for (int i = 0; i < 12; i++) {            // double the cross products
-        const uint64_t hi = t[i] >> 63;
-        t[i] = (t[i] << 1) | top;
-        top = hi;
-    }
-    u128 c = 0;
-    for (int i = 0; i < 6; i++) {             // add the squares
-        const u128 sq = (u128)a.l[i] * a.l[i];
-        c += (u128)t[2 * i] + (uint64_t)sq;
-        t[2 * i] = (uint64_t)c;
-        c >>= 64;
-        c += (u128)t[2 * i + 1] + (uint64_t)(sq >> 64);
-        t[2 * i + 1] = (uint64_t)c;
-        c >>= 64;
-    }
-    for (int i = 0; i < 6; i++) {             // Montgomery reduction, one limb at a time
-        const uint64_t m = t[i] * HN0;
-        u128 d = 0;
-        for (int j = 0; j < 6; j++) {
-            d += (u128)m * HP[j] + t[i + j];
-            t[i + j] = (uint64_t)d;
-            d >>= 64;
-        }
-        for (int j = i + 6; j < 13 && d; j++) {
-            d += t[j];
-            t[j] = (uint64_t)d;
-            d >>= 64;
-        }
-    }
-    uint64_t r[6];
-    std::memcpy(r, t + 6, 48);
-    if (t[12] || geq(r, HP)) sub_p(r);
-    std::memcpy(o.l, r, 48);
-}
+// o = a^2 (Montgomery), canonical a.
+inline void sqr(hfp& o, const hfp& a) { mul(o, a, a); }
 
 // R^3 mod p (R = 2^384): a Montgomery multiplication by it maps U^-1 to U^-1 R^2.
 static const uint64_t HR3[6] = {0xed48ac6bd94ca1e0ULL, 0x315f831e03a7adf8ULL, 0x9a53352a615e29ddULL,

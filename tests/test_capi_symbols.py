@@ -135,9 +135,9 @@ def test_inversion_correction_tables():
 
 def test_host_fold_arithmetic(gpu_binding):
     """The host arithmetic that folds the MSM window sums and normalises the
-    result (no GPU involved): the squaring and the variable-time inversion
-    against Python integers, including 0, 1, p - 1, R and non-canonical
-    inputs in [p, 2^384)."""
+    result (no GPU involved): the multiplication, the squaring and the
+    variable-time inversion against Python integers, including 0, 1, p - 1, R
+    and non-canonical inputs in [p, 2^384)."""
     import random
     P = 0x1a0111ea397fe69a4b1ba7b6434bacd764774b84f38512bf6730d2a0f6b0f6241eabfffeb153ffffb9feffffffffaaab
     RM = (1 << 384) % P
@@ -152,9 +152,15 @@ def test_host_fold_arithmetic(gpu_binding):
     sqr_out = (C.c_char * (48 * n))()
     assert lib.catmsm_host_fp_inv(inv_out, buf, C.c_size_t(n)) == 0
     assert lib.catmsm_host_fp_sqr(sqr_out, buf, C.c_size_t(n)) == 0
+    others = vals[1:] + vals[:1]                 # b[i] = a[i + 1]: every edge value meets others
+    buf_b = (C.c_char * (48 * n)).from_buffer(bytearray(b"".join(v.to_bytes(48, "little") for v in others)))
+    mul_out = (C.c_char * (48 * n))()
+    assert lib.catmsm_host_fp_mul(mul_out, buf, buf_b, C.c_size_t(n)) == 0
     rinv = pow(RM, -1, P)
     for i, v in enumerate(vals):
         a = v % P * rinv % P                    # the field element v represents
         exp_inv = 0 if a == 0 else pow(a, -1, P) * RM % P
         assert int.from_bytes(bytes(inv_out[48 * i:48 * i + 48]), "little") == exp_inv, hex(v)
         assert int.from_bytes(bytes(sqr_out[48 * i:48 * i + 48]), "little") == (v % P) ** 2 * rinv % P, hex(v)
+        assert int.from_bytes(bytes(mul_out[48 * i:48 * i + 48]), "little") == \
+            (v % P) * (others[i] % P) * rinv % P, (hex(v), hex(others[i]))
