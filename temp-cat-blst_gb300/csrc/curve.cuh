@@ -364,6 +364,86 @@ static __device__ __noinline__ void jac_mult_glv(jac& out, const jac& P, const u
     out = acc;
 }
 
+// Width-5 NAF of a value below 2^128 (4 little-endian words): digits d_i in
+// {0, +-1, +-3, ..., +-15} with value = sum_i d_i 2^i and at most one nonzero
+// digit in any five consecutive positions (density ~1/6).  Returns the number
+// of digits, at most 129: subtracting a negative digit can carry the value
+// past 2^128 once, after which every step halves it.
+__device__ __forceinline__ int wnaf5_128(int8_t* d, const uint32_t* k)
+{
+    uint32_t w0 = k[0], w1 = k[1], w2 = k[2], w3 = k[3], w4 = 0;
+    int len = 0;
+#pragma unroll 1
+    for (int i = 0; i < 130 && (w0 | w1 | w2 | w3 | w4); i++) {
+        int v = 0;
+        if (w0 & 1u) {
+            v = (int)(w0 & 31u);
+            if (v > 16) v -= 32;
+            if (v > 0) {
+                w0 -= (uint32_t)v;                   // the low five bits are v: no borrow
+            } else {
+                uint64_t s = (uint64_t)w0 + (uint32_t)(-v);
+                w0 = (uint32_t)s;
+                s = (s >> 32) + w1; w1 = (uint32_t)s;
+                s = (s >> 32) + w2; w2 = (uint32_t)s;
+                s = (s >> 32) + w3; w3 = (uint32_t)s;
+                w4 += (uint32_t)(s >> 32);
+            }
+        }
+        d[i] = (int8_t)v;
+        len = i + 1;
+        w0 = (w0 >> 1) | (w1 << 31);
+        w1 = (w1 >> 1) | (w2 << 31);
+        w2 = (w2 >> 1) | (w3 << 31);
+        w3 = (w3 >> 1) | (w4 << 31);
+        w4 >>= 1;
+    }
+    return len;
+}
+
+// jac_mult_glv for lanes that all multiply by one scalar (k1, k2): each half
+// in width-5 NAF over the odd multiples P, 3P, ..., 15P (one doubling and
+// seven additions) and phi of them, ~129 doublings and ~50 additions against
+// 133 and ~57 for the fixed windows.  The digit positions depend on the
+// scalar, so lanes with different scalars would diverge at every addition;
+// jac_mult_glv serves those.
+static __device__ __noinline__ void jac_mult_glv_shared(jac& out, const jac& P, const uint32_t* k1,
+                                                        const uint32_t* k2)
+{
+    int8_t d1[130], d2[130];
+    const int n1 = wnaf5_128(d1, k1), n2 = wnaf5_128(d2, k2);
+    jac T[8];                                    // T[i] = (2 i + 1) P
+    jac P2 = P;
+    jac_dbl(P2);
+    T[0] = P;
+#pragma unroll 1
+    for (int i = 1; i < 8; i++) {
+        T[i] = T[i - 1];
+        jac_add(T[i], P2);
+    }
+    fp beta;
+#pragma unroll
+    for (int i = 0; i < 12; i++) beta.v[i] = FP_BETA[i];
+    jac acc;
+    jac_set_inf(acc);
+    for (int i = max(n1, n2) - 1; i >= 0; i--) {
+        jac_dbl(acc);
+        const int a = i < n1 ? d1[i] : 0, b = i < n2 ? d2[i] : 0;
+        if (a) {
+            jac t = T[(a > 0 ? a : -a) >> 1];
+            if (a < 0) jac_neg(t);
+            jac_add(acc, t);
+        }
+        if (b) {
+            jac t = T[(b > 0 ? b : -b) >> 1];
+            fp_mul(t.x, t.x, beta);
+            if (b < 0) jac_neg(t);
+            jac_add(acc, t);
+        }
+    }
+    out = acc;
+}
+
 // ---------------------------------------------------------------------------
 // Quad point operations: four consecutive lanes (a quad) hold the same
 // operands and perform one XYZZ addition or doubling together.  At each step

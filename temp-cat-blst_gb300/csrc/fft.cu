@@ -16,9 +16,12 @@
 //                      level (a batch of transforms fills the GPU where one
 //                      small transform cannot); inside a job, threads map
 //                      first onto the non-trivial butterflies (j >= 1, one
-//                      GLV scalar multiplication in signed 5-bit windows
-//                      each), then onto the
+//                      GLV scalar multiplication each), then onto the
 //                      j == 0 butterflies, so a warp rarely mixes the two.
+//                      Early stages (32 or more active groups) put the lanes
+//                      of a warp on one root (width-5 NAF halves); later
+//                      ones on consecutive roots (signed 5-bit fixed
+//                      windows, the same digit positions for every root).
 //                      Launches small enough to fit one wave at four lanes
 //                      per butterfly use quad point operations.
 //   k_fft_finish_multi the inverse 1/n scale (one GLV multiplication per
@@ -137,10 +140,21 @@ __global__ void __launch_bounds__(64) k_fft_stage_multi(jac* __restrict__ a, con
     const uint32_t groups = J.n / len;
     const uint32_t active = min(groups, J.xn);
     const uint32_t nontriv = active * (half - 1);
+    // Non-trivial butterflies: with at least 32 active groups (a multiple of
+    // 32), the group index runs fastest, so the lanes of a warp share j and
+    // its root and take the width-5 NAF multiplication; otherwise j runs
+    // fastest and the lanes, on different roots, keep the fixed windows.
     uint32_t g, j;
+    bool shared = false;
     if (b < nontriv) {
-        g = b / (half - 1);
-        j = 1 + b % (half - 1);
+        if (!Quad && (active & 31u) == 0) {
+            j = 1 + b / active;
+            g = b % active;
+            shared = true;
+        } else {
+            g = b / (half - 1);
+            j = 1 + b % (half - 1);
+        }
     } else {
         g = b - nontriv;
         j = 0;
@@ -160,6 +174,7 @@ __global__ void __launch_bounds__(64) k_fft_stage_multi(jac* __restrict__ a, con
         if (J.inv_from_fwd) idx = J.n - idx;
         const uint32_t* r = glv + 8 * (size_t)(J.glv_off + idx);
         if (Quad) jac_mult_glv_quad(v, v, r, r + 4, ql);
+        else if (shared) jac_mult_glv_shared(v, v, r, r + 4);
         else jac_mult_glv(v, v, r, r + 4);
     }
     jac s = u;
@@ -195,7 +210,7 @@ __global__ void __launch_bounds__(64) k_fft_finish_multi(jac* __restrict__ a, co
     if (do_scale && J.scaled) {
         const uint32_t* r = glv + 8 * (size_t)(J.glv_off + J.n);
         if (Quad) jac_mult_glv_quad(v, v, r, r + 4, ql);
-        else jac_mult_glv(v, v, r, r + 4);
+        else jac_mult_glv_shared(v, v, r, r + 4);        // one scale per job, shared by its lanes
     }
     if (jac_is_inf(v)) {
         jac_set_inf(v);
