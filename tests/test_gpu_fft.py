@@ -212,11 +212,15 @@ def test_fft_truncated_prefix_matches_oracle(gpu, oracle):
                 assert oracle.serialize(got[144 * i:144 * i + 144]) == oracle.serialize(exp[144 * i:144 * i + 144]), (n, xn, i)
 
 
-def test_fft_truncated_prefix_large_equals_full(gpu, oracle, synth):
-    """n = 2^16, xn = 5000: the early stages run only the active groups (quads
-    while they fit one wave, one lane per butterfly after); the outputs equal
-    the full forward transform of the same input."""
-    n, xn = 1 << 16, 5000
+@pytest.mark.parametrize("xn", [5000, 8192])
+def test_fft_truncated_prefix_large_equals_full(gpu, oracle, synth, xn):
+    """n = 2^16: the early stages run only the active groups (quads while they
+    fit one wave, one lane per butterfly after); the outputs equal the full
+    forward transform of the same input.  xn = 8192: at the second level 8192
+    of 16384 groups are active (a multiple of 32, too many butterflies for
+    quads), so the lanes of a warp share one root over bit-reversed groups,
+    where the full transform maps its groups in order."""
+    n = 1 << 16
     aff = gpu.points_from_scalars(synth.point_scalars(73, xn), xn)
     jac = oracle.jacobian_randomize(73, xn, aff) + bytes(144 * (n - xn))
     d = gpu.fr_fft_domain_init(n)[1]
