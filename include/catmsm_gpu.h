@@ -336,19 +336,28 @@ int catmsm_basis_autotune(void *basis, size_t nmsm, const size_t *counts, const 
 /* ---- Serving engine (no reference counterpart): continuous batching of MSM
  * and FFT requests over a resident basis (catmsm_basis_create) on one GPU.
  * `workers` threads each own a stream and a workspace; a free worker takes
- * the queued requests at the head of the queue as one batch (all queued MSMs,
- * or all queued FFTs, up to a point cap), so requests that arrive while other
- * batches run join at the next batch boundary and batches of different
- * workers overlap on the device.  A batch starts only while the estimated
- * device memory of all in-flight batches stays within hbm_budget_bytes (0 =
- * 64 GiB; a single request above the budget runs alone).
+ * the oldest queued request and, as one batch, every other queued request of
+ * its size class (MSMs: k in the same power-of-four band; FFTs: the same n),
+ * up to a point cap, so requests that arrive while other batches run join at
+ * the next batch boundary and batches of different workers overlap on the
+ * device.  Worker 0 runs on the highest-priority stream and takes the oldest
+ * large request (an MSM of >= 2^20 points, an FFT of >= 2^14) first; MSMs of
+ * >= 2^18 points and a batch of one MSM run through the plain pipeline over
+ * the basis points, smaller batched MSMs over its fixed-base tables.  A batch
+ * starts only while the estimated device memory of all in-flight batches
+ * stays within hbm_budget_bytes (0 = 64 GiB; a single request above the
+ * budget runs alone).
  * submit_msm: MSM over the first k basis points with k 32-byte scalars;
  * submit_fft: blst_p1_fft_with_domain semantics with mode 0 forward, 1 inverse,
  * 2 inverse unscaled, in place on `values`.  Input buffers must stay valid
  * until wait returns.  Both return a ticket (> 0) or -1 on invalid input.
  * wait blocks until the ticket completes, writes the MSM result (Jacobian) to
  * msm_out if not NULL and times_ms[0..1] = queueing and total latency in ms
- * (host steady clock) if not NULL, and returns 0 or a cudaError_t value.
+ * (host steady clock) if not NULL, and returns 0 or a cudaError_t value.  A
+ * ticket is waited once: an unknown ticket, or one another wait call already
+ * holds or has returned, gives cudaErrorInvalidValue.  destroy runs every
+ * queued request to completion and frees the ones never waited; no wait may
+ * be in progress when it is called, nor follow it.
  * The basis must not be reconfigured or destroyed while a server uses it. */
 void *catmsm_server_create(void *basis, size_t workers, size_t hbm_budget_bytes);
 void catmsm_server_destroy(void *server);

@@ -61,6 +61,7 @@ struct Request {
     double t_submit = 0, t_start = 0, t_done = 0;
     int status = 0;
     bool done = false;
+    bool claimed = false;               // a wait call owns it (a ticket is waited once)
 };
 
 struct Server;
@@ -381,12 +382,15 @@ int catmsm_server_wait(void* server, int64_t ticket, blst_p1* msm_out, double* t
     if (!s) return (int)cudaErrorInvalidValue;
     Request* r = nullptr;
     {
+        // The lock is released while waiting and a submit may rehash the
+        // map, so the entry is erased by key afterwards, not by iterator.
         std::unique_lock<std::mutex> lk(s->mu);
         auto it = s->reqs.find(ticket);
-        if (it == s->reqs.end()) return (int)cudaErrorInvalidValue;
+        if (it == s->reqs.end() || it->second->claimed) return (int)cudaErrorInvalidValue;
         r = it->second;
+        r->claimed = true;
         s->cv_done.wait(lk, [&] { return r->done; });
-        s->reqs.erase(it);
+        s->reqs.erase(ticket);
     }
     if (msm_out && r->type == 0) *msm_out = r->result;
     if (times_ms) {
