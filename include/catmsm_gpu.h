@@ -320,7 +320,10 @@ int catmsm_p1s_mult_pippenger_noalloc(blst_p1 *ret, const blst_p1_affine *points
  * Results are Jacobian blst_p1 (not normalised; z = 0 for infinity), as the
  * reference MSM returns them.  use_graph != 0 replays the batch's device
  * sequence as one CUDA graph launch (captured on first use per batch size).
- * Calls on one basis must not overlap (one stream, one workspace per basis).
+ * A basis has one stream and one workspace: calls on it from several host
+ * threads (batches, set_config, config, autotune) are serialised by the
+ * library and must be made with the basis's device current
+ * (cudaErrorInvalidDevice otherwise).
  * catmsm_basis_autotune times (window, chunk) candidates on a caller batch,
  * keeps the fastest, and remembers it per (GPU, n, nmsm, points-per-MSM
  * class) in the text file $CATMSM_TUNE_CACHE (default ~/.cache/catmsm_tune.txt);

@@ -245,7 +245,8 @@ struct Basis {
     cudaStream_t stream = nullptr;
     DevBuf points, table, tmp;
     BatchWork work;
-    std::mutex mu;     // serialises table rebuilds against running batches
+    std::mutex mu;     // serialises the direct calls (batches, reconfiguration, autotuning): they share the
+                       // basis's workspace and stream, and a rebuild replaces the tables a batch reads
 };
 
 static cudaError_t build_tables(Basis* b, uint32_t c)
@@ -535,18 +536,29 @@ int catmsm_basis_config(void* handle, size_t* window, size_t* chunk)
 {
     Basis* b = (Basis*)handle;
     if (!b) return (int)cudaErrorInvalidValue;
+    std::lock_guard<std::mutex> lk(b->mu);
     if (window) *window = b->c;
     if (chunk) *chunk = b->L;
+    return 0;
+}
+
+// catmsm_basis_set_config with b->mu held by the caller.
+static int set_config_locked(Basis* b, size_t window, size_t chunk)
+{
+    if (window < 2 || window > 20 || chunk < 2 || chunk > 256) return (int)cudaErrorInvalidValue;
+    b->L = (uint32_t)chunk;
+    if (window != b->c) return (int)build_tables(b, (uint32_t)window);
     return 0;
 }
 
 int catmsm_basis_set_config(void* handle, size_t window, size_t chunk)
 {
     Basis* b = (Basis*)handle;
-    if (!b || window < 2 || window > 20 || chunk < 2 || chunk > 256) return (int)cudaErrorInvalidValue;
-    b->L = (uint32_t)chunk;
-    if (window != b->c) return (int)build_tables(b, (uint32_t)window);
-    return 0;
+    if (!b) return (int)cudaErrorInvalidValue;
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev != b->device) return (int)cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lk(b->mu);
+    return set_config_locked(b, window, chunk);
 }
 
 int catmsm_basis_msm_batch(void* handle, blst_p1* out, size_t nmsm, const size_t* counts, const blst_byte* scalars,
@@ -564,11 +576,14 @@ int catmsm_basis_autotune(void* handle, size_t nmsm, const size_t* counts, const
 {
     Basis* b = (Basis*)handle;
     if (!b || !counts || !scalars || nmsm == 0) return (int)cudaErrorInvalidValue;
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev != b->device) return (int)cudaErrorInvalidDevice;
     size_t pairs = 0;
     for (size_t j = 0; j < nmsm; j++) pairs += counts[j];
     const std::string key = tune_key(b->n, (uint32_t)nmsm, pairs);
     uint32_t c = 0, L = 0;
-    if (!force && tune_lookup(key, &c, &L)) return catmsm_basis_set_config(b, c, L);
+    std::lock_guard<std::mutex> lk(b->mu);       // the whole sweep: it reconfigures and runs the basis
+    if (!force && tune_lookup(key, &c, &L)) return set_config_locked(b, c, L);
     std::vector<blst_p1> out(nmsm);
     cudaEvent_t e0, e1;
     CATMSM_CHECK(cudaEventCreate(&e0));
@@ -579,7 +594,7 @@ int catmsm_basis_autotune(void* handle, size_t nmsm, const size_t* counts, const
     const uint32_t ls[] = {8, 16, 32, 48, 64, 96, 128, 192, 256};   // chunk lengths (96 measured best at 1024 x ~1.4k)
     for (uint32_t cc : cs) {
         for (uint32_t ll : ls) {
-            if (catmsm_basis_set_config(b, cc, ll) != 0) continue;
+            if (set_config_locked(b, cc, ll) != 0) continue;
             if (run_batch(b, &b->work, b->stream, out.data(), (uint32_t)nmsm, counts, scalars, true, false) !=
                 cudaSuccess)
                 continue;
@@ -604,7 +619,7 @@ int catmsm_basis_autotune(void* handle, size_t nmsm, const size_t* counts, const
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    int rc = catmsm_basis_set_config(b, bc, bl);
+    int rc = set_config_locked(b, bc, bl);
     if (rc == 0) tune_store(key, bc, bl);
     return rc;
 }
