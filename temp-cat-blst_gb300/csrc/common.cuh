@@ -3,6 +3,7 @@
 // error helpers.  All public entry points are synchronous and fail closed.
 #pragma once
 #include <cuda_runtime.h>
+#include <atomic>
 #include <cstring>
 #include <cstddef>
 #include <cstdint>
@@ -18,17 +19,22 @@ namespace catmsm {
 constexpr int kGB300SMs = 152;
 
 // SM count of the current device, queried once per device (devices past the
-// cache are queried on every call); grids are sized in multiples of it.
+// cache are queried on every call); grids are sized in multiples of it.  The
+// cache is shared by every calling thread: atomic entries, each written with
+// the same value by whichever thread gets there first.
 inline int device_sms()
 {
-    static int cache[64] = {0};
+    static std::atomic<int> cache[64];
     int dev = -1;
     if (cudaGetDevice(&dev) != cudaSuccess) dev = -1;
-    if (dev >= 0 && dev < 64 && cache[dev] > 0) return cache[dev];
+    if (dev >= 0 && dev < 64) {
+        const int v = cache[dev].load(std::memory_order_relaxed);
+        if (v > 0) return v;
+    }
     int sms = 0;
     if (dev < 0 || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
         return kGB300SMs;   // only reached with a broken context; the next launch reports the error
-    if (dev < 64) cache[dev] = sms;
+    if (dev < 64) cache[dev].store(sms, std::memory_order_relaxed);
     return sms;
 }
 

@@ -229,15 +229,18 @@ __global__ void __launch_bounds__(64) k_fft_finish_multi(jac* __restrict__ a, co
 // multiplier work).
 static size_t fft_quad_max()
 {
-    static size_t by_dev[64] = {0};
+    static std::atomic<size_t> by_dev[64];          // shared by every calling thread
     int dev = 0;
     cudaGetDevice(&dev);
-    if (dev >= 0 && dev < 64 && by_dev[dev]) return by_dev[dev];
+    if (dev >= 0 && dev < 64) {
+        const size_t v = by_dev[dev].load(std::memory_order_relaxed);
+        if (v) return v;
+    }
     int sms = 0, per_sm = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fft_stage_multi<true>, 64, 0);
     size_t v = (sms > 0 && per_sm > 0) ? (size_t)sms * per_sm * 64 / 4 : (size_t)device_sms() * 64;
-    if (dev >= 0 && dev < 64) by_dev[dev] = v;
+    if (dev >= 0 && dev < 64) by_dev[dev].store(v, std::memory_order_relaxed);
     return v;
 }
 

@@ -947,11 +947,14 @@ void msm_reduce_pair(const void* inA, const void* inQ, uint32_t m, uint32_t D, v
 // larger L (fewer chunk carries to join).
 static uint32_t accumulate_chunk(size_t nD)
 {
-    static int slots_by_dev[64] = {0}, sms_by_dev[64] = {0};
+    // Shared by every calling thread: sms is stored before slots (release)
+    // and read after it (acquire), so a thread that sees slots sees sms.
+    static std::atomic<int> slots_by_dev[64], sms_by_dev[64];
     int dev = 0;
     cudaGetDevice(&dev);
     const bool cached = dev >= 0 && dev < 64;
-    int slots = cached ? slots_by_dev[dev] : 0, sms = cached ? sms_by_dev[dev] : 0;
+    int slots = cached ? slots_by_dev[dev].load(std::memory_order_acquire) : 0;
+    int sms = cached ? sms_by_dev[dev].load(std::memory_order_relaxed) : 0;
     if (slots == 0) {
         int per_sm = 0;
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -962,8 +965,8 @@ static uint32_t accumulate_chunk(size_t nD)
         }
         slots = sms * per_sm * 128;
         if (cached) {
-            slots_by_dev[dev] = slots;
-            sms_by_dev[dev] = sms;
+            sms_by_dev[dev].store(sms, std::memory_order_relaxed);
+            slots_by_dev[dev].store(slots, std::memory_order_release);
         }
     }
     const double W = (double)nD / slots;
